@@ -1,0 +1,116 @@
+/*
+ * voxgpu.h — C ABI of the GB300 (sm_103a) voxel geometry pipeline.
+ *
+ * Two groups of entry points:
+ *
+ * 1. The device-resident world API (vp_*). A world mirrors one reference
+ *    ChunkSet (src/chunkset.h:29-55): chunk size 2^root_bitw, 2^max_bitw[i]
+ *    chunks per axis, every chunk stored as its RLE stream in HBM, plus the
+ *    sun-shadow map. vp_world_rebuild runs, for every chunk, what the
+ *    reference's mesher thread does per chunk in chunkset_manage
+ *    (src/chunkset.c:246-507): decode, then either the quad mesh
+ *    (chunk_make_mesh, src/chunkset/mesher.c:184-357) or the exposure mask,
+ *    LOD chain and splat lists (chunk_make_mask / chunk_mask_downsample /
+ *    chunk_make_splatlist, src/chunkset/mesher.c:377-536) — in one batched
+ *    launch instead of one OpenMP iteration per chunk.
+ *
+ * 2. Drop-in replacements with the reference's own names and signatures,
+ *    declared in voxgpu_dropin.h.
+ *
+ * Every function returns 0 (VP_OK) or a negative VP_E* code; no function
+ * aborts the process. Outputs are bit-identical to the reference C code.
+ */
+#ifndef VOXGPU_H
+#define VOXGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define VP_API __attribute__((visibility("default")))
+#else
+#define VP_API
+#endif
+
+#define VP_OK 0
+#define VP_EINVAL (-1)       /* bad argument or malformed RLE stream */
+#define VP_ENOMEM (-2)       /* device or host allocation failed */
+#define VP_ECUDA (-3)        /* a CUDA call failed; see vp_last_cuda_error */
+#define VP_EOVERFLOW (-4)    /* output arena too small and growth refused */
+#define VP_ETIMEOUT (-5)     /* a bounded device wait ran out */
+#define VP_EUNSUPPORTED (-6) /* chunk size or level count not supported */
+#define VP_EBUSY (-7)        /* admission refused: not enough free HBM */
+
+#define VP_MAX_LEVELS 8      /* LOD levels 0..7 in one result record */
+
+typedef struct vp_ctx vp_ctx;
+typedef struct vp_world vp_world;
+
+/* Result of one chunk; offsets index the world's output arenas. Item counts
+ * are in the reference's units: int16 elements for splats and vertices
+ * (svl_items, mesh_vbo_items, src/chunkset.h:108-117), u32 for indices. */
+typedef struct vp_chunk_result {
+	uint64_t svl_off;
+	uint64_t vbo_off;
+	uint64_t ibo_off;
+	uint32_t svl_items[VP_MAX_LEVELS];
+	uint32_t svl_total;
+	uint32_t vbo_items;
+	uint32_t ibo_items;
+	uint32_t status;
+} vp_chunk_result;
+
+/* Rebuild flags */
+#define VP_REBUILD_PERSISTENT 1u /* persistent CTAs + device work queue */
+
+VP_API const char *vp_strerror(int code);
+VP_API const char *vp_last_cuda_error(void);
+
+/* A context owns one CUDA stream on `device`. */
+VP_API int vp_ctx_create(int device, vp_ctx **out);
+VP_API void vp_ctx_destroy(vp_ctx *ctx);
+VP_API void *vp_ctx_stream(vp_ctx *ctx);       /* the cudaStream_t */
+VP_API int vp_ctx_sync(vp_ctx *ctx);
+
+/* Worlds. root_bitw 3..6 (chunks of 8^3 .. 64^3). */
+VP_API int vp_world_create(vp_ctx *ctx, int root_bitw, const int max_bitw[3], vp_world **out);
+VP_API void vp_world_destroy(vp_world *w);
+
+/* Copy a whole world from host memory: the RLE streams of every chunk
+ * (pool words, per-chunk word offsets and lengths including the 0
+ * terminator) and the shadow map (shadow_len elements, zero padded past the
+ * map; reads past shadow_len return 0). Streams are validated: every run
+ * count >= 1, runs sum to root^3, a single 0 terminator. */
+VP_API int vp_world_upload(vp_world *w, const uint32_t *pool, uint64_t pool_words, const uint64_t *off,
+			   const uint32_t *len, const uint16_t *shadow, uint64_t shadow_len, uint32_t shadow_w);
+
+/* Per chunk: 1 = quad mesh (near chunk, ChunkMD.make_mesh), 0 = splats.
+ * NULL = every chunk splats. */
+VP_API int vp_world_set_modes(vp_world *w, const uint8_t *make_mesh);
+
+/* Enqueue a full rebuild on the context stream (asynchronous). */
+VP_API int vp_world_rebuild(vp_world *w, int lod_max, unsigned flags);
+/* Wait for the rebuild; grow the output arenas and rebuild again if any
+ * chunk overflowed. */
+VP_API int vp_world_finish(vp_world *w);
+
+VP_API int vp_world_results(vp_world *w, vp_chunk_result *out, uint32_t n);
+VP_API int vp_world_read_svl(vp_world *w, uint64_t off, uint64_t n, int16_t *dst);
+VP_API int vp_world_read_vbo(vp_world *w, uint64_t off, uint64_t n, int16_t *dst);
+VP_API int vp_world_read_ibo(vp_world *w, uint64_t off, uint64_t n, uint32_t *dst);
+
+/* Kernel timing: with timing on, every rebuild records CUDA events around
+ * its kernels on the context stream; vp_world_kernel_ms returns the summed
+ * milliseconds of the shell pass and the geometry pass since the last call
+ * (waits for the stream) and resets them. */
+VP_API int vp_ctx_set_timing(vp_ctx *ctx, int on);
+VP_API int vp_world_kernel_ms(vp_world *w, double *shell_ms, double *geometry_ms, uint32_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,211 @@
+"""ctypes bindings of the oracle libraries (TEST INFRASTRUCTURE ONLY).
+
+`OracleWorld` wraps the C restatement (libvpo.so); `RefWorld` wraps the
+reference's own sources compiled by build_ref.sh (libvpref.so, present only
+where the reference tree is). Both load a `voxplat_gb300.worldgen.World`.
+"""
+import ctypes
+
+import numpy as np
+
+from . import build
+
+c_u32p = ctypes.POINTER(ctypes.c_uint32)
+_vpo = None
+_ref = None
+
+
+def _vp(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def vpo_lib():
+    global _vpo
+    if _vpo is None:
+        lib = ctypes.CDLL(build.build_oracle())
+        V = ctypes.c_void_p
+        lib.vpo_world_new.restype = V
+        lib.vpo_world_new.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_uint32]
+        lib.vpo_world_free.argtypes = [V]
+        lib.vpo_world_set_rle.argtypes = [V, ctypes.c_uint32, V, ctypes.c_uint32]
+        lib.vpo_world_set_shadow.argtypes = [V, V, ctypes.c_uint64]
+        lib.vpo_world_voxels.restype = ctypes.POINTER(ctypes.c_uint8)
+        lib.vpo_world_voxels.argtypes = [V, ctypes.c_uint32]
+        lib.vpo_chunk_splats.restype = ctypes.c_uint32
+        lib.vpo_chunk_splats.argtypes = [V, ctypes.c_uint32, ctypes.c_int, V, V, V, V]
+        lib.vpo_make_mesh.argtypes = [V, ctypes.c_uint32, V, V, V, V]
+        lib.vpo_make_mask.argtypes = [V, ctypes.c_uint32, V]
+        lib.vpo_rle_encode.restype = ctypes.c_uint32
+        lib.vpo_rle_encode.argtypes = [V, ctypes.c_uint32, V]
+        lib.vpo_rle_decode.restype = ctypes.c_uint32
+        lib.vpo_rle_decode.argtypes = [V, V, ctypes.c_uint32]
+        lib.vpo_edit_sphere.restype = ctypes.c_uint32
+        lib.vpo_edit_sphere.argtypes = [V, V, ctypes.c_uint32, ctypes.c_uint8, V]
+        lib.vpo_group_node.restype = ctypes.c_uint64
+        lib.vpo_group_node.argtypes = [V, ctypes.c_int, V, V, V, V]
+        _vpo = lib
+    return _vpo
+
+
+def ref_lib():
+    """The compiled reference, or None where the reference tree is absent."""
+    global _ref
+    if _ref is None:
+        path = build.build_ref()
+        if path is None:
+            return None
+        lib = ctypes.CDLL(path)
+        V = ctypes.c_void_p
+        lib.vpref_world_new.restype = V
+        lib.vpref_world_new.argtypes = [ctypes.c_int] * 4 + [ctypes.c_uint32]
+        lib.vpref_set_shadow.argtypes = [V, V, ctypes.c_uint64]
+        lib.vpref_get_shadow.argtypes = [V, V, ctypes.c_uint64]
+        lib.vpref_set_chunk_rle.argtypes = [V, ctypes.c_uint32, V, ctypes.c_uint32]
+        lib.vpref_chunk_splats.restype = ctypes.c_uint32
+        lib.vpref_chunk_splats.argtypes = [V, ctypes.c_uint32, ctypes.c_int, V, V, V, V]
+        lib.vpref_chunk_mesh.argtypes = [V, ctypes.c_uint32, V, V, V, V]
+        lib.vpref_edit_sphere.argtypes = [V] + [ctypes.c_int32] * 3 + [ctypes.c_uint32, ctypes.c_uint8]
+        lib.vpref_chunk_voxels.argtypes = [V, ctypes.c_uint32, V]
+        lib.vpref_chunk_dirty.argtypes = [V, ctypes.c_uint32]
+        lib.vpref_clear_dirty.argtypes = [V]
+        lib.vpref_rle_compress.restype = ctypes.c_uint32
+        lib.vpref_rle_compress.argtypes = [V, ctypes.c_uint32, V]
+        lib.vpref_rle_decompress.restype = ctypes.c_uint32
+        lib.vpref_rle_decompress.argtypes = [V, V, ctypes.c_uint32]
+        _ref = lib
+    return _ref
+
+
+def _splat_cap(R, lod_max):
+    return 4 * sum(((R >> l) + 1) ** 3 for l in range(lod_max + 1)) + 16
+
+
+def _mesh_cap(R):
+    return 3 * R ** 3 + 16  # faces
+
+
+class _Base:
+    def splats(self, c, lod_max=4):
+        """(int16 svl array, per-level int16 item counts) of chunk c."""
+        R = self.R
+        S3 = (R + 1) ** 3
+        geom = np.zeros(_splat_cap(R, lod_max), np.int16)
+        items = np.zeros(max(lod_max + 1, 8), np.uint32)
+        mask = np.zeros(S3, np.uint8)
+        work = np.zeros(S3, np.uint8)
+        n = self._splats(c, lod_max, geom, items, mask, work)
+        return geom[:n].copy(), items[:lod_max + 1].copy()
+
+    def mesh(self, c):
+        """(int16 vbo, uint32 ibo) of chunk c."""
+        F = _mesh_cap(self.R)
+        vbo = np.zeros(16 * F, np.int16)
+        ibo = np.zeros(6 * F, np.uint32)
+        nv = np.zeros(1, np.uint32)
+        ni = np.zeros(1, np.uint32)
+        self._mesh(c, vbo, nv, ibo, ni)
+        return vbo[:int(nv[0])].copy(), ibo[:int(ni[0])].copy()
+
+
+class OracleWorld(_Base):
+    def __init__(self, world):
+        lib = vpo_lib()
+        self.lib = lib
+        self.R = world.R
+        mb = (ctypes.c_int * 3)(*world.max_bitw)
+        self.h = lib.vpo_world_new(world.root_bitw, mb, world.pad_rows)
+        self.nchunks = world.nchunks
+        for c in range(world.nchunks):
+            s = np.ascontiguousarray(world.chunk_rle(c))
+            lib.vpo_world_set_rle(self.h, c, _vp(s), len(s))
+        lib.vpo_world_set_shadow(self.h, _vp(world.shadow), len(world.shadow))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.vpo_world_free(self.h)
+            self.h = None
+
+    def _splats(self, c, lod_max, geom, items, mask, work):
+        return self.lib.vpo_chunk_splats(self.h, c, lod_max, _vp(geom), _vp(items), _vp(mask), _vp(work))
+
+    def _mesh(self, c, vbo, nv, ibo, ni):
+        self.lib.vpo_make_mesh(self.h, c, _vp(vbo), _vp(nv), _vp(ibo), _vp(ni))
+
+    def mask(self, c):
+        m = np.zeros((self.R + 1) ** 3, np.uint8)
+        self.lib.vpo_make_mask(self.h, c, _vp(m))
+        return m
+
+    def voxels(self, c):
+        p = self.lib.vpo_world_voxels(self.h, c)
+        return np.ctypeslib.as_array(p, shape=(self.R ** 3,)).copy()
+
+    def edit_sphere(self, ws, r, v):
+        ws = np.asarray(ws, np.int32)
+        dirty = np.zeros(self.nchunks, np.uint8)
+        self.lib.vpo_edit_sphere(self.h, _vp(ws), r, v, _vp(dirty))
+        return dirty
+
+    def shadow(self, n):
+        # shadow pointer lives in the struct; read via a helper world copy
+        raise NotImplementedError
+
+
+class RefWorld(_Base):
+    def __init__(self, world):
+        lib = ref_lib()
+        if lib is None:
+            raise RuntimeError("reference tree not present")
+        self.lib = lib
+        self.R = world.R
+        self.nchunks = world.nchunks
+        bx, by, bz = world.max_bitw
+        self.h = lib.vpref_world_new(world.root_bitw, bx, by, bz, world.pad_rows)
+        for c in range(world.nchunks):
+            s = np.ascontiguousarray(world.chunk_rle(c))
+            lib.vpref_set_chunk_rle(self.h, c, _vp(s), len(s))
+        lib.vpref_set_shadow(self.h, _vp(world.shadow), len(world.shadow))
+        self.shadow_len = len(world.shadow)
+
+    def _splats(self, c, lod_max, geom, items, mask, work):
+        return self.lib.vpref_chunk_splats(self.h, c, lod_max, _vp(geom), _vp(items), _vp(mask), _vp(work))
+
+    def _mesh(self, c, vbo, nv, ibo, ni):
+        self.lib.vpref_chunk_mesh(self.h, c, _vp(vbo), _vp(nv), _vp(ibo), _vp(ni))
+
+    def voxels(self, c):
+        out = np.zeros(self.R ** 3, np.uint8)
+        self.lib.vpref_chunk_voxels(self.h, c, _vp(out))
+        return out
+
+    def edit_sphere(self, ws, r, v):
+        self.lib.vpref_clear_dirty(self.h)
+        self.lib.vpref_edit_sphere(self.h, int(ws[0]), int(ws[1]), int(ws[2]), r, v)
+        return np.array([self.lib.vpref_chunk_dirty(self.h, c) for c in range(self.nchunks)], np.uint8)
+
+    def shadow(self):
+        out = np.zeros(self.shadow_len, np.uint16)
+        self.lib.vpref_get_shadow(self.h, _vp(out), self.shadow_len)
+        return out
+
+
+def ref_rle_compress(vox):
+    lib = ref_lib()
+    vox = np.ascontiguousarray(vox, np.uint8)
+    out = np.zeros(len(vox) + 2, np.uint32)
+    n = lib.vpref_rle_compress(_vp(vox), len(vox), _vp(out))
+    return out[:n].copy()
+
+
+def vpo_rle_encode(vox):
+    vox = np.ascontiguousarray(vox, np.uint8)
+    out = np.zeros(len(vox) + 2, np.uint32)
+    n = vpo_lib().vpo_rle_encode(_vp(vox), len(vox), _vp(out))
+    return out[:n].copy()
+
+
+def vpo_rle_decode(words, n):
+    words = np.ascontiguousarray(words, np.uint32)
+    out = np.zeros(n, np.uint8)
+    vpo_lib().vpo_rle_decode(_vp(words), _vp(out), n)
+    return out

@@ -1,0 +1,524 @@
+/*
+ * oracle/vpo.c — CPU restatement of voxplat's per-chunk geometry pipeline.
+ *
+ * TEST INFRASTRUCTURE ONLY (the parity oracle; see vpo.h). Scalar C that
+ * follows the reference loop by loop; each function cites the reference
+ * function it restates (kosshi-net/voxplat 0.11, paths relative to the
+ * project root).
+ */
+#include "vpo.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define RLE_MASK 0xFFFFFFu
+#define RLE_SHIFT 24
+
+/* src/chunkset/rle.c:44-87 */
+uint32_t vpo_rle_encode(const uint8_t *vox, uint32_t n, uint32_t *out)
+{
+	uint32_t count = 1, b = 0;
+	uint8_t last = vox[0];
+	for (uint32_t i = 1; i < n; i++) {
+		uint8_t cur = vox[i];
+		if (cur == last && count < RLE_MASK) {
+			count++;
+			continue;
+		}
+		out[b++] = count | ((uint32_t)last << RLE_SHIFT);
+		count = 1;
+		last = cur;
+	}
+	out[b++] = count | ((uint32_t)last << RLE_SHIFT);
+	out[b++] = 0;
+	return b;
+}
+
+/* src/chunkset/rle.c:90-117. The first word is always consumed (do-while);
+ * decoding stops at the first zero word after it. Writes past `cap` are
+ * dropped (the reference sizes its buffer from the last encoded length). */
+uint32_t vpo_rle_decode(const uint32_t *words, uint8_t *out, uint32_t cap)
+{
+	uint32_t i = 0, b = 0;
+	do {
+		uint32_t count = words[i] & RLE_MASK;
+		uint8_t item = (uint8_t)(words[i] >> RLE_SHIFT);
+		uint32_t n = count;
+		if (b >= cap) n = 0;
+		else if (n > cap - b) n = cap - b;
+		memset(out + b, item, n);
+		b += count;
+	} while (words[++i]);
+	return b;
+}
+
+vpo_world *vpo_world_new(int root_bitw, const int max_bitw[3], uint32_t pad_rows)
+{
+	vpo_world *w = (vpo_world *)calloc(1, sizeof(*w));
+	w->root_bitw = root_bitw;
+	w->R = 1 << root_bitw;
+	for (int i = 0; i < 3; i++) {
+		w->max_bitw[i] = max_bitw[i];
+		w->max[i] = 1 << max_bitw[i];
+	}
+	w->nchunks = (uint32_t)w->max[0] * w->max[1] * w->max[2];
+	w->rle = (uint32_t **)calloc(w->nchunks, sizeof(uint32_t *));
+	w->rle_len = (uint32_t *)calloc(w->nchunks, sizeof(uint32_t));
+	w->vox = (uint8_t **)calloc(w->nchunks, sizeof(uint8_t *));
+	/* src/chunkset/shadow.h:26-43 sizes; padded and zeroed here. */
+	w->shadow_w = ((uint32_t)w->max[0] << root_bitw) + ((uint32_t)w->max[1] << root_bitw);
+	w->shadow_z = (uint32_t)w->max[2] << root_bitw;
+	w->shadow_len = (uint64_t)w->shadow_w * (w->shadow_z + pad_rows);
+	w->shadow = (uint16_t *)calloc(w->shadow_len, sizeof(uint16_t));
+	/* chunkset_clear (src/chunkset.c:85-121): every chunk starts as air. */
+	uint32_t N = (uint32_t)w->R * w->R * w->R;
+	for (uint32_t c = 0; c < w->nchunks; c++) {
+		w->rle[c] = (uint32_t *)malloc(2 * sizeof(uint32_t));
+		w->rle[c][0] = N;
+		w->rle[c][1] = 0;
+		w->rle_len[c] = 2;
+	}
+	return w;
+}
+
+void vpo_world_free(vpo_world *w)
+{
+	if (!w) return;
+	for (uint32_t c = 0; c < w->nchunks; c++) {
+		free(w->rle[c]);
+		free(w->vox[c]);
+	}
+	free(w->rle);
+	free(w->rle_len);
+	free(w->vox);
+	free(w->shadow);
+	free(w);
+}
+
+void vpo_world_set_rle(vpo_world *w, uint32_t c, const uint32_t *words, uint32_t n)
+{
+	free(w->rle[c]);
+	free(w->vox[c]);
+	w->vox[c] = NULL;
+	w->rle[c] = (uint32_t *)malloc((size_t)n * sizeof(uint32_t));
+	memcpy(w->rle[c], words, (size_t)n * sizeof(uint32_t));
+	w->rle_len[c] = n;
+}
+
+void vpo_world_set_shadow(vpo_world *w, const uint16_t *map, uint64_t n)
+{
+	if (n > w->shadow_len) n = w->shadow_len;
+	memcpy(w->shadow, map, n * sizeof(uint16_t));
+}
+
+/* chunk_open_ro (src/chunkset.c:133-152): decode lazily and keep the voxels.
+ * Safe to call from several threads: a racing decode loses the swap. */
+const uint8_t *vpo_world_voxels(vpo_world *w, uint32_t c)
+{
+	uint8_t *v = __atomic_load_n(&w->vox[c], __ATOMIC_ACQUIRE);
+	if (v) return v;
+	uint32_t N = (uint32_t)w->R * w->R * w->R;
+	uint8_t *d = (uint8_t *)malloc(N);
+	vpo_rle_decode(w->rle[c], d, N);
+	uint8_t *expected = NULL;
+	if (!__atomic_compare_exchange_n(&w->vox[c], &expected, d, 0, __ATOMIC_ACQ_REL,
+					 __ATOMIC_ACQUIRE)) {
+		free(d);
+		return expected;
+	}
+	return d;
+}
+
+/* chunk_compress (src/chunkset.c:213-230): re-encode the decoded voxels. */
+void vpo_world_compress(vpo_world *w, uint32_t c)
+{
+	if (!w->vox[c]) return;
+	uint32_t N = (uint32_t)w->R * w->R * w->R;
+	uint32_t *tmp = (uint32_t *)malloc(((size_t)N + 2) * sizeof(uint32_t));
+	uint32_t n = vpo_rle_encode(w->vox[c], N, tmp);
+	free(w->rle[c]);
+	w->rle[c] = (uint32_t *)realloc(tmp, (size_t)n * sizeof(uint32_t));
+	w->rle_len[c] = n;
+}
+
+/* flatten3 (src/chunkset.c:124-126) */
+uint32_t vpo_flatten3(const vpo_world *w, const uint32_t cv[3])
+{
+	return ((cv[2] << w->max_bitw[1] | cv[1]) << w->max_bitw[0]) | cv[0];
+}
+
+/* chunkset_edit_read (src/chunkset/edit.c:10-36): out of world reads air. */
+uint8_t vpo_world_read(vpo_world *w, const uint32_t ws[3])
+{
+	for (int i = 0; i < 3; i++)
+		if (ws[i] >= ((uint32_t)w->max[i] << w->root_bitw)) return 0;
+	uint32_t cv[3], vv[3];
+	for (int i = 0; i < 3; i++) {
+		cv[i] = ws[i] >> w->root_bitw;
+		vv[i] = ws[i] - (cv[i] << w->root_bitw);
+	}
+	const uint8_t *v = vpo_world_voxels(w, vpo_flatten3(w, cv));
+	return v[(vv[2] << (2 * w->root_bitw)) | (vv[1] << w->root_bitw) | vv[0]];
+}
+
+static inline uint16_t shadow_at(const vpo_world *w, uint32_t idx)
+{
+	return (uint64_t)idx < w->shadow_len ? w->shadow[idx] : 0;
+}
+
+/* shadow_index + shadow_sample (src/chunkset/shadow.h:45-63); all index
+ * arithmetic in uint32 as in the reference. */
+int vpo_shadow_sample(const vpo_world *w, const uint32_t ws[3])
+{
+	uint32_t idx = (ws[0] + ws[1]) + w->shadow_w * ws[2];
+	uint32_t lim = ws[1] + 1;
+	return !(shadow_at(w, idx) < lim && shadow_at(w, idx + 1) < lim);
+}
+
+/* shadow_sample_normal (src/chunkset/shadow.h:65-75) */
+int vpo_shadow_sample_normal(const vpo_world *w, const uint32_t ws[3])
+{
+	uint32_t idx = (ws[0] + ws[1]) + w->shadow_w * ws[2];
+	uint32_t lim = ws[1] + 1;
+	return !(shadow_at(w, idx) < lim && shadow_at(w, idx - 1) < lim);
+}
+
+/* shadow_place_update (src/chunkset/shadow.h:77-89) */
+void vpo_shadow_place_update(vpo_world *w, const uint32_t ws[3])
+{
+	if (vpo_shadow_sample(w, ws)) return;
+	uint32_t idx = (ws[0] + ws[1]) + w->shadow_w * ws[2];
+	if ((uint64_t)idx < w->shadow_len) w->shadow[idx] = (uint16_t)ws[1];
+}
+
+/* The +x/+y/+z neighbours of chunk c, or NULL past the world edge
+ * (src/chunkset/mesher.c:391-402 / 200-211). */
+static void plus_neighbours(vpo_world *w, uint32_t c, const uint8_t *nb[3], uint32_t off[3])
+{
+	uint32_t cv[3];
+	cv[0] = c & (uint32_t)(w->max[0] - 1);
+	cv[1] = (c >> w->max_bitw[0]) & (uint32_t)(w->max[1] - 1);
+	cv[2] = c >> (w->max_bitw[0] + w->max_bitw[1]);
+	for (int i = 0; i < 3; i++) off[i] = cv[i];
+	for (int i = 0; i < 3; i++) {
+		cv[i]++;
+		if (cv[i] + 1 > (uint32_t)w->max[i])
+			nb[i] = NULL;
+		else
+			nb[i] = vpo_world_voxels(w, vpo_flatten3(w, cv));
+		cv[i]--;
+	}
+}
+
+/* chunk_make_mask (src/chunkset/mesher.c:377-456) */
+void vpo_make_mask(vpo_world *w, uint32_t c, uint8_t *mask)
+{
+	const uint8_t *nb[3];
+	uint32_t off[3];
+	plus_neighbours(w, c, nb, off);
+	const uint8_t *v = vpo_world_voxels(w, c);
+	const uint32_t R = (uint32_t)w->R, rb = (uint32_t)w->root_bitw, S = R + 1;
+	uint32_t AC[3], Ai = 0;
+	for (AC[2] = 0; AC[2] < R; AC[2]++)
+		for (AC[1] = 0; AC[1] < R; AC[1]++)
+			for (AC[0] = 0; AC[0] < R; AC[0]++, Ai++) {
+				uint8_t A = v[Ai];
+				uint32_t shift = 0;
+				for (int i = 0; i < 3; i++, shift += rb) {
+					uint8_t B;
+					if (AC[i] + 1 == R)
+						B = nb[i] ? nb[i][Ai - ((R - 1) << shift)] : 0;
+					else
+						B = v[Ai + (1u << shift)];
+					if (!A == !B) continue;
+					uint32_t MC[3] = {AC[0], AC[1], AC[2]};
+					MC[i] += (A == 0);
+					mask[(MC[2] * S + MC[1]) * S + MC[0]] = A | B;
+				}
+			}
+}
+
+/* chunk_mask_downsample (src/chunkset/mesher.c:460-493): the last nonzero
+ * child in z,y,x scan order wins. */
+void vpo_mask_downsample(int R, int level, const uint8_t *mask, uint8_t *work)
+{
+	const uint32_t S = (uint32_t)R + 1;
+	const uint32_t range = ((uint32_t)R >> (level - 1)) + 1;
+	for (uint32_t z = 0; z < range; z++)
+		for (uint32_t y = 0; y < range; y++)
+			for (uint32_t x = 0; x < range; x++) {
+				uint8_t m = mask[(z * S + y) * S + x];
+				if (!m) continue;
+				work[((z >> 1) * S + (y >> 1)) * S + (x >> 1)] = m;
+			}
+}
+
+/* chunk_make_splatlist (src/chunkset/mesher.c:497-536). Returns items
+ * written (the reference adds them to *geometry_items). */
+uint32_t vpo_make_splatlist(vpo_world *w, uint32_t c, int level, const uint8_t *mask, int16_t *geom)
+{
+	uint32_t cv[3];
+	cv[0] = c & (uint32_t)(w->max[0] - 1);
+	cv[1] = (c >> w->max_bitw[0]) & (uint32_t)(w->max[1] - 1);
+	cv[2] = c >> (w->max_bitw[0] + w->max_bitw[1]);
+	const uint32_t R = (uint32_t)w->R, S = R + 1;
+	const uint32_t range = (R >> level) + 1;
+	uint32_t v = 0;
+	for (uint32_t z = 0; z < range; z++)
+		for (uint32_t y = 0; y < range; y++)
+			for (uint32_t x = 0; x < range; x++) {
+				uint8_t m = mask[(z * S + y) * S + x];
+				if (!m) continue;
+				uint32_t AC[3] = {x, y, z}, ws[3];
+				for (int j = 0; j < 3; j++) {
+					ws[j] = (cv[j] << w->root_bitw) + (AC[j] << level);
+					geom[v++] = (int16_t)(uint16_t)ws[j];
+				}
+				if (level)
+					for (int j = 0; j < 3; j++) ws[j] += 1u << level;
+				geom[v++] = (int16_t)(uint16_t)(m | (vpo_shadow_sample(w, ws) << 6));
+			}
+	return v;
+}
+
+/* chunkset_manage's far-chunk sequence (src/chunkset.c:321-459). */
+uint32_t vpo_chunk_splats(vpo_world *w, uint32_t c, int lod_max, int16_t *geom, uint32_t *items,
+			  uint8_t *mask, uint8_t *work)
+{
+	const size_t S3 = (size_t)(w->R + 1) * (w->R + 1) * (w->R + 1);
+	memset(mask, 0, S3);
+	memset(work, 0, S3);
+	vpo_make_mask(w, c, mask);
+	uint32_t total = vpo_make_splatlist(w, c, 0, mask, geom);
+	items[0] = total;
+	for (int l = 1; l <= lod_max; l++) {
+		uint8_t *src = (l & 1) ? mask : work;
+		uint8_t *dst = (l & 1) ? work : mask;
+		if (l >= 2) memset(dst, 0, S3);
+		vpo_mask_downsample(w->R, l, src, dst);
+		items[l] = vpo_make_splatlist(w, c, l, dst, geom + total);
+		total += items[l];
+	}
+	return total;
+}
+
+/* Vertex offsets of the three visible quad orientations (the first 36
+ * entries of lutv, src/chunkset/mesher.c:19-33) and the index pattern with
+ * AO rotation and back-face variants (luti, src/chunkset/mesher.c:53-66). */
+static const uint8_t quad_offset[3][4][3] = {
+	{{1, 0, 0}, {1, 0, 1}, {1, 1, 1}, {1, 1, 0}},
+	{{0, 1, 0}, {1, 1, 0}, {1, 1, 1}, {0, 1, 1}},
+	{{1, 0, 1}, {0, 0, 1}, {0, 1, 1}, {1, 1, 1}},
+};
+static const uint8_t quad_index[24] = {0, 3, 1, 2, 1, 3, 3, 2, 0, 1, 0, 2,
+				       1, 3, 0, 3, 1, 2, 0, 2, 3, 2, 0, 1};
+
+/* sample_ao (mesher.c:72-116) and sample_ao_border (mesher.c:119-171):
+ * edge samples -u, -v, +u, +v and corner samples (-,-), (+,-), (+,+), (-,+)
+ * around the air voxel, in the two axes other than the face axis. Interior
+ * voxels read the chunk; border voxels read the world. */
+static void sample_ao(vpo_world *w, const uint8_t *v, const uint32_t off[3], const uint32_t AIR[3],
+		      int face, int border, uint8_t aon[4], uint8_t aoc[4])
+{
+	int uv[2], d = 0;
+	const uint32_t rb = (uint32_t)w->root_bitw;
+	uint32_t base[3];
+	for (int k = 0; k < 3; k++) base[k] = border ? (off[k] << rb) + AIR[k] : AIR[k];
+#define AO_READ(O) (border ? !!vpo_world_read(w, O) \
+			   : !!v[((O)[2] << (2 * rb)) | ((O)[1] << rb) | (O)[0]])
+	for (int a = 0; a < 3; a++) {
+		if (a == face) continue;
+		uv[d] = a;
+		uint32_t O[3];
+		memcpy(O, base, sizeof(O));
+		O[a]++;
+		aon[d + 2] = AO_READ(O);
+		memcpy(O, base, sizeof(O));
+		O[a]--;
+		aon[d] = AO_READ(O);
+		d++;
+	}
+	static const int cs[4][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
+	for (int k = 0; k < 4; k++) {
+		uint32_t O[3];
+		memcpy(O, base, sizeof(O));
+		O[uv[0]] += (uint32_t)cs[k][0];
+		O[uv[1]] += (uint32_t)cs[k][1];
+		aoc[k] = AO_READ(O);
+	}
+#undef AO_READ
+}
+
+/* chunk_make_mesh (src/chunkset/mesher.c:184-357) */
+void vpo_make_mesh(vpo_world *w, uint32_t c, int16_t *geom, uint32_t *vbo_items, uint32_t *index,
+		   uint32_t *ibo_items)
+{
+	const uint8_t *nb[3];
+	uint32_t off[3];
+	plus_neighbours(w, c, nb, off);
+	const uint8_t *vx = vpo_world_voxels(w, c);
+	const uint32_t R = (uint32_t)w->R, rb = (uint32_t)w->root_bitw;
+	uint32_t v = 0, nidx = 0, vertices = 0;
+	uint32_t AC[3], Ai = 0;
+	for (AC[2] = 0; AC[2] < R; AC[2]++)
+		for (AC[1] = 0; AC[1] < R; AC[1]++)
+			for (AC[0] = 0; AC[0] < R; AC[0]++, Ai++) {
+				uint8_t A = vx[Ai];
+				uint32_t shift = 0;
+				for (int i = 0; i < 3; i++, shift += rb) {
+					uint8_t B;
+					if (AC[i] == R - 1)
+						B = nb[i] ? nb[i][Ai - ((R - 1) << shift)] : 0;
+					else
+						B = vx[Ai + (1u << shift)];
+					if (!A == !B) continue;
+					uint32_t AIR[3] = {AC[0], AC[1], AC[2]};
+					AIR[i] += (B == 0);
+					uint32_t BLOCK[3] = {AC[0], AC[1], AC[2]};
+					BLOCK[i] += (A == 0);
+					int border = 0;
+					for (int k = 0; k < 3; k++)
+						if (AC[k] == 0 || AC[k] == R - 1) border = 1;
+					uint8_t aon[4], aoc[4];
+					sample_ao(w, vx, off, AIR, i, border, aon, aoc);
+					uint8_t va[4];
+					uint8_t e0 = (uint8_t)((aon[0] + aon[1]) | aoc[0]);
+					uint8_t e1 = (uint8_t)((aon[1] + aon[2]) | aoc[1]);
+					uint8_t e2 = (uint8_t)((aon[2] + aon[3]) | aoc[2]);
+					uint8_t e3 = (uint8_t)((aon[3] + aon[0]) | aoc[3]);
+					if (i == 0) {
+						va[0] = e0; va[3] = e1; va[2] = e2; va[1] = e3;
+					} else if (i == 1) {
+						va[0] = e0; va[1] = e1; va[2] = e2; va[3] = e3;
+					} else {
+						va[1] = e0; va[0] = e1; va[3] = e2; va[2] = e3;
+					}
+					int rotate = (va[0] + va[2] < va[1] + va[3]) ? 6 : 0;
+					uint32_t ws[3];
+					for (int k = 0; k < 3; k++) ws[k] = (off[k] << rb) + BLOCK[k];
+					int normal = (A == 0);
+					int shadow = 0;
+					if (i == 0 && normal)
+						shadow = vpo_shadow_sample_normal(w, ws);
+					else if (i == 1 && !normal)
+						shadow = vpo_shadow_sample(w, ws);
+					ws[i] -= (uint32_t)normal;
+					int diamond = 3;
+					if (i == 2) {
+						shadow = 0;
+						uint32_t sws[3] = {ws[0], ws[1], ws[2]};
+						if (!B) sws[2] += 1;
+						diamond = (!vpo_shadow_sample(w, sws)) << 1;
+						sws[1] -= 1;
+						diamond |= !vpo_shadow_sample(w, sws);
+					}
+					for (int vert = 0; vert < 4; vert++) {
+						for (int k = 0; k < 3; k++)
+							geom[v++] = (int16_t)(uint16_t)(ws[k] + quad_offset[i][vert][k]);
+						int word = (A | B) | (va[vert] << 6) | ((i + 3 * normal) << 8) |
+							   (vert << 11) | (shadow << 13) | (diamond << 14);
+						geom[v++] = (int16_t)(uint16_t)word;
+					}
+					for (int k = 0; k < 6; k++)
+						index[nidx++] = vertices + quad_index[normal * 12 + k + rotate];
+					vertices += 4;
+				}
+			}
+	*vbo_items = v;
+	*ibo_items = nidx;
+}
+
+/* chunkset_get_chunks_in_aabb (src/chunkset/edit.c:89-126), chunk_ws_inside
+ * (:129-140), chunk_ws_write (:143-176) and chunkset_edit_sphere
+ * (:179-244). The distance test is the reference's float sqrtf compare. */
+uint32_t vpo_edit_sphere(vpo_world *w, const int32_t ws[3], uint32_t radius, uint8_t voxel,
+			 uint8_t *dirty)
+{
+	const int rb = w->root_bitw, R = w->R;
+	int32_t mn[3], mx[3];
+	for (int i = 0; i < 3; i++) {
+		mn[i] = ws[i] - (int32_t)radius - 1;
+		mx[i] = ws[i] + (int32_t)radius + 1;
+	}
+	int16_t cmin[3], cmax[3];
+	for (int i = 0; i < 3; i++) {
+		cmax[i] = (int16_t)(mx[i] >> rb);
+		cmin[i] = (int16_t)(mn[i] >> rb);
+	}
+	uint32_t list[1024];
+	uint32_t n = 0;
+	int16_t cs[3];
+	for (cs[0] = cmin[0]; cs[0] <= cmax[0]; ++cs[0])
+		for (cs[1] = cmin[1]; cs[1] <= cmax[1]; ++cs[1])
+			for (cs[2] = cmin[2]; cs[2] <= cmax[2]; ++cs[2]) {
+				int ok = 1;
+				for (int i = 0; i < 3; i++)
+					if (cs[i] < 0 || cs[i] >= w->max[i]) ok = 0;
+				if (!ok || n >= 1024) continue;
+				uint32_t cv[3] = {(uint16_t)cs[0], (uint16_t)cs[1], (uint16_t)cs[2]};
+				list[n++] = vpo_flatten3(w, cv);
+			}
+	if (!n) return 0;
+	const float fr = (float)radius;
+	for (uint32_t k = 0; k < n; k++) {
+		uint32_t c = list[k];
+		uint8_t *vx = (uint8_t *)vpo_world_voxels(w, c);
+		int32_t lo[3];
+		lo[0] = (int32_t)((c & (uint32_t)(w->max[0] - 1)) << rb);
+		lo[1] = (int32_t)(((c >> w->max_bitw[0]) & (uint32_t)(w->max[1] - 1)) << rb);
+		lo[2] = (int32_t)((c >> (w->max_bitw[0] + w->max_bitw[1])) << rb);
+		int32_t u[3];
+		for (u[0] = mn[0]; u[0] < mx[0]; u[0]++)
+			for (u[1] = mn[1]; u[1] < mx[1]; u[1]++)
+				for (u[2] = mn[2]; u[2] < mx[2]; u[2]++) {
+					float d0 = (float)ws[0] - (float)u[0];
+					float d1 = (float)ws[1] - (float)u[1];
+					float d2 = (float)ws[2] - (float)u[2];
+					float dist = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+					if (!(dist < fr)) continue;
+					int inside = 1;
+					for (int i = 0; i < 3; i++)
+						if (u[i] < lo[i] || u[i] + 1 > lo[i] + R) inside = 0;
+					if (!inside) continue;
+					if (u[1] >= 2)
+						vx[(uint32_t)(u[0] - lo[0]) |
+						   ((uint32_t)(u[1] - lo[1]) << rb) |
+						   ((uint32_t)(u[2] - lo[2]) << (2 * rb))] = voxel;
+					if (voxel) {
+						uint32_t uu[3] = {(uint32_t)u[0], (uint32_t)u[1], (uint32_t)u[2]};
+						vpo_shadow_place_update(w, uu);
+					}
+				}
+		vpo_world_compress(w, c);
+	}
+	if (dirty)
+		for (uint32_t k = 0; k < n; k++) dirty[list[k]] = 1;
+	return n;
+}
+
+/* gfx_update_svl's per-node concatenation (src/gfx/vsplat.c:209-331). */
+uint64_t vpo_group_node(const vpo_world *w, int lod, const uint32_t node[3], int16_t *const *svl,
+			const uint32_t *const *svl_items, int16_t *out)
+{
+	uint32_t lo[3], hi[3];
+	for (int i = 0; i < 3; i++) {
+		lo[i] = node[i] << lod;
+		hi[i] = (node[i] + 1) << lod;
+		if (hi[i] > (uint32_t)w->max[i]) hi[i] = (uint32_t)w->max[i];
+	}
+	uint64_t total = 0;
+	uint32_t s[3];
+	for (s[0] = lo[0]; s[0] < hi[0]; s[0]++)
+		for (s[1] = lo[1]; s[1] < hi[1]; s[1]++)
+			for (s[2] = lo[2]; s[2] < hi[2]; s[2]++) {
+				uint32_t c = vpo_flatten3(w, s);
+				uint32_t n = svl_items[c][lod];
+				if (!n) continue;
+				uint32_t start = 0;
+				for (int k = 0; k < lod; k++) start += svl_items[c][k];
+				memcpy(out + total, svl[c] + start, (size_t)n * sizeof(int16_t));
+				total += n;
+			}
+	return total;
+}

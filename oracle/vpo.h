@@ -1,0 +1,94 @@
+/*
+ * oracle/vpo.h — CPU restatement of voxplat's per-chunk geometry pipeline.
+ *
+ * TEST INFRASTRUCTURE ONLY. This is the parity oracle: tests, the smoke
+ * check and the benchmark's CPU-baseline leg call it to check or time the
+ * CUDA path. The product never links it.
+ *
+ * Each function restates one reference function (file:line in
+ * kosshi-net/voxplat 0.11) in plain scalar C. The restatement is pinned
+ * against the unmodified reference sources, compiled by oracle/build_ref.sh
+ * into oracle/_ref/, through golden fixtures under tests/golden/.
+ *
+ * Conventions that make the reference's undefined corners deterministic (the
+ * same conventions hold on the GPU):
+ *   - the shadow map is zero padded after its last row, and a read at an
+ *     index at or past the padded length returns 0;
+ *   - a chunk's +x/+y/+z neighbour past the world edge is all air (the
+ *     reference's null chunk, src/chunkset/mesher.c:391-402);
+ *   - chunk_make_mask's early-out (src/chunkset/mesher.c:404-409), which
+ *     reads an uninitialised neighbour copy, is not taken: the full face
+ *     scan runs, which is what the early-out is meant to be equivalent to.
+ */
+#ifndef VPO_H
+#define VPO_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct vpo_world {
+	int root_bitw, R;
+	int max_bitw[3], max[3];
+	uint32_t nchunks;
+	uint32_t **rle;      /* per chunk: owned stream incl. terminator */
+	uint32_t *rle_len;   /* words incl. terminator */
+	uint8_t **vox;       /* per chunk: decoded voxels, filled lazily */
+	uint16_t *shadow;    /* padded map */
+	uint64_t shadow_len; /* padded length in elements */
+	uint32_t shadow_w;   /* X + Y world extent */
+	uint32_t shadow_z;
+} vpo_world;
+
+/* rle.c */
+uint32_t vpo_rle_encode(const uint8_t *vox, uint32_t n, uint32_t *out);
+uint32_t vpo_rle_decode(const uint32_t *words, uint8_t *out, uint32_t cap);
+
+/* world state */
+vpo_world *vpo_world_new(int root_bitw, const int max_bitw[3], uint32_t pad_rows);
+void vpo_world_free(vpo_world *w);
+void vpo_world_set_rle(vpo_world *w, uint32_t chunk, const uint32_t *words, uint32_t n);
+void vpo_world_set_shadow(vpo_world *w, const uint16_t *map, uint64_t n);
+const uint8_t *vpo_world_voxels(vpo_world *w, uint32_t chunk);
+void vpo_world_compress(vpo_world *w, uint32_t chunk);
+uint32_t vpo_flatten3(const vpo_world *w, const uint32_t cv[3]);
+uint8_t vpo_world_read(vpo_world *w, const uint32_t ws[3]);
+
+/* shadow.h */
+int vpo_shadow_sample(const vpo_world *w, const uint32_t ws[3]);
+int vpo_shadow_sample_normal(const vpo_world *w, const uint32_t ws[3]);
+void vpo_shadow_place_update(vpo_world *w, const uint32_t ws[3]);
+
+/* mesher.c */
+void vpo_make_mask(vpo_world *w, uint32_t chunk, uint8_t *mask);
+void vpo_mask_downsample(int R, int level, const uint8_t *mask, uint8_t *work);
+uint32_t vpo_make_splatlist(vpo_world *w, uint32_t chunk, int level, const uint8_t *mask,
+			    int16_t *geom);
+void vpo_make_mesh(vpo_world *w, uint32_t chunk, int16_t *vbo, uint32_t *vbo_items,
+		   uint32_t *ibo, uint32_t *ibo_items);
+
+/* chunkset.c:367-459 splat sequence: mask, L0, then downsample + splat per
+ * level up to lod_max. Returns total int16 items; per-level counts in items.
+ * `mask` and `work` are (R+1)^3 bytes of caller scratch. */
+uint32_t vpo_chunk_splats(vpo_world *w, uint32_t chunk, int lod_max, int16_t *geom,
+			  uint32_t *items, uint8_t *mask, uint8_t *work);
+
+/* edit.c:179-244 sphere edit; marks dirty[c] = 1 for every chunk in the
+ * edit's AABB (dirty may be NULL). Returns the number of such chunks. */
+uint32_t vpo_edit_sphere(vpo_world *w, const int32_t ws[3], uint32_t radius, uint8_t voxel,
+			 uint8_t *dirty);
+
+/* vsplat.c:209-331 grouping: concatenation of LOD-`lod` segments of the
+ * member chunks of octree node `node`. seg_off/seg_items give, per chunk, the
+ * int16 offset and item count of that chunk's level-`lod` segment in `svl`
+ * (segment pointers may differ per chunk, so svl is an array of pointers).
+ * Returns int16 items written. */
+uint64_t vpo_group_node(const vpo_world *w, int lod, const uint32_t node[3],
+			int16_t *const *svl, const uint32_t *const *svl_items, int16_t *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

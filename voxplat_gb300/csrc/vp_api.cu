@@ -1,0 +1,466 @@
+/*
+ * vp_api.cu — the C ABI (include/voxgpu.h): contexts, device-resident worlds,
+ * batched rebuilds, result readback and kernel timing.
+ */
+#include "voxgpu.h"
+#include "vp_geometry.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+using namespace vp;
+
+namespace {
+
+thread_local std::string g_cuda_err;
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+	char buf[256];
+	snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+	g_cuda_err = buf;
+	return e == cudaErrorMemoryAllocation ? VP_ENOMEM : VP_ECUDA;
+}
+
+#define CK(call)                                                  \
+	do {                                                      \
+		cudaError_t e_ = (call);                          \
+		if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+	} while (0)
+
+template <typename T>
+int dev_alloc(T **p, size_t n)
+{
+	*p = nullptr;
+	if (n == 0) n = 1;
+	cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+	if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+	return VP_OK;
+}
+
+template <typename T>
+void dev_free(T *&p)
+{
+	if (p) cudaFree((void *)p);
+	p = nullptr;
+}
+
+} // namespace
+
+struct vp_ctx {
+	int device;
+	cudaStream_t stream;
+	int timing;
+	int sm_count;
+};
+
+struct vp_world {
+	vp_ctx *ctx;
+	int root_bitw;
+	int max_bitw[3];
+	uint32_t nchunks;
+	uint32_t *d_pool = nullptr;
+	uint64_t pool_words = 0;
+	uint64_t *d_off = nullptr;
+	uint32_t *d_len = nullptr;
+	uint16_t *d_shadow = nullptr;
+	uint64_t shadow_len = 0;
+	uint32_t shadow_w = 0;
+	uint64_t *d_shell_bits = nullptr;
+	uint8_t *d_shell_col = nullptr;
+	SetDesc *d_set = nullptr;
+	WorkItem *d_items = nullptr;
+	std::vector<uint8_t> modes;
+	bool items_dirty = true;
+	ChunkOut *d_outs = nullptr;
+	unsigned int *d_queue = nullptr;
+	unsigned long long *d_cursors = nullptr; /* svl, vbo, ibo */
+	void *d_arena[3] = {nullptr, nullptr, nullptr};
+	uint64_t cap[3] = {0, 0, 0};             /* 16-byte units */
+	int last_lod = 4;
+	unsigned last_flags = 0;
+	bool uploaded = false;
+	std::vector<cudaEvent_t> ev;             /* pairs per kernel */
+	std::vector<int> ev_kind;                /* 0 shell, 1 geometry */
+	double ms[2] = {0, 0};
+	uint32_t launches = 0;
+};
+
+extern "C" {
+
+VP_API const char *vp_strerror(int code)
+{
+	switch (code) {
+	case VP_OK: return "ok";
+	case VP_EINVAL: return "invalid argument";
+	case VP_ENOMEM: return "out of memory";
+	case VP_ECUDA: return "CUDA error";
+	case VP_EOVERFLOW: return "output overflow";
+	case VP_ETIMEOUT: return "device wait timed out";
+	case VP_EUNSUPPORTED: return "unsupported configuration";
+	case VP_EBUSY: return "admission refused";
+	default: return "unknown error";
+	}
+}
+
+VP_API const char *vp_last_cuda_error(void) { return g_cuda_err.c_str(); }
+
+VP_API int vp_ctx_create(int device, vp_ctx **out)
+{
+	if (!out) return VP_EINVAL;
+	*out = nullptr;
+	CK(cudaSetDevice(device));
+	vp_ctx *c = new vp_ctx();
+	c->device = device;
+	c->timing = 0;
+	cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+	if (e != cudaSuccess) {
+		delete c;
+		return cuda_fail(e, "cudaStreamCreate");
+	}
+	cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+	*out = c;
+	return VP_OK;
+}
+
+VP_API void vp_ctx_destroy(vp_ctx *c)
+{
+	if (!c) return;
+	cudaSetDevice(c->device);
+	cudaStreamSynchronize(c->stream);
+	cudaStreamDestroy(c->stream);
+	delete c;
+}
+
+VP_API void *vp_ctx_stream(vp_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+VP_API int vp_ctx_sync(vp_ctx *c)
+{
+	if (!c) return VP_EINVAL;
+	CK(cudaStreamSynchronize(c->stream));
+	return VP_OK;
+}
+
+VP_API int vp_ctx_set_timing(vp_ctx *c, int on)
+{
+	if (!c) return VP_EINVAL;
+	c->timing = on ? 1 : 0;
+	return VP_OK;
+}
+
+VP_API int vp_world_create(vp_ctx *ctx, int root_bitw, const int max_bitw[3], vp_world **out)
+{
+	if (!ctx || !out || !max_bitw) return VP_EINVAL;
+	*out = nullptr;
+	if (geometry_smem_bytes(root_bitw) == 0) return VP_EUNSUPPORTED;
+	for (int i = 0; i < 3; i++)
+		if (max_bitw[i] < 0 || max_bitw[i] > 12) return VP_EINVAL;
+	if (max_bitw[0] + max_bitw[1] + max_bitw[2] > 24) return VP_EUNSUPPORTED;
+	CK(cudaSetDevice(ctx->device));
+	vp_world *w = new vp_world();
+	w->ctx = ctx;
+	w->root_bitw = root_bitw;
+	for (int i = 0; i < 3; i++) w->max_bitw[i] = max_bitw[i];
+	w->nchunks = 1u << (max_bitw[0] + max_bitw[1] + max_bitw[2]);
+	w->modes.assign(w->nchunks, 0);
+	int rc = VP_OK;
+	if ((rc = dev_alloc(&w->d_off, w->nchunks)) || (rc = dev_alloc(&w->d_len, w->nchunks)) ||
+	    (rc = dev_alloc(&w->d_shell_bits, (size_t)w->nchunks * shell_words_per_chunk(root_bitw))) ||
+	    (rc = dev_alloc(&w->d_shell_col, (size_t)w->nchunks * shell_cols_per_chunk(root_bitw))) ||
+	    (rc = dev_alloc(&w->d_set, 1)) || (rc = dev_alloc(&w->d_items, w->nchunks)) ||
+	    (rc = dev_alloc(&w->d_outs, w->nchunks)) || (rc = dev_alloc(&w->d_queue, 1)) ||
+	    (rc = dev_alloc(&w->d_cursors, 3))) {
+		vp_world_destroy(w);
+		return rc;
+	}
+	*out = w;
+	return VP_OK;
+}
+
+VP_API void vp_world_destroy(vp_world *w)
+{
+	if (!w) return;
+	cudaSetDevice(w->ctx->device);
+	cudaStreamSynchronize(w->ctx->stream);
+	dev_free(w->d_pool);
+	dev_free(w->d_off);
+	dev_free(w->d_len);
+	dev_free(w->d_shadow);
+	dev_free(w->d_shell_bits);
+	dev_free(w->d_shell_col);
+	dev_free(w->d_set);
+	dev_free(w->d_items);
+	dev_free(w->d_outs);
+	dev_free(w->d_queue);
+	dev_free(w->d_cursors);
+	for (int a = 0; a < 3; a++) dev_free(w->d_arena[a]);
+	for (cudaEvent_t e : w->ev) cudaEventDestroy(e);
+	delete w;
+}
+
+static int validate_stream(const uint32_t *s, uint32_t n, uint64_t N)
+{
+	if (n < 2 || s[n - 1] != 0) return VP_EINVAL;
+	uint64_t sum = 0;
+	for (uint32_t i = 0; i + 1 < n; i++) {
+		uint32_t c = s[i] & 0xFFFFFFu;
+		if (c == 0) return VP_EINVAL;
+		sum += c;
+	}
+	return sum == N ? VP_OK : VP_EINVAL;
+}
+
+static int upload_setdesc(vp_world *w)
+{
+	SetDesc d;
+	memset(&d, 0, sizeof(d));
+	d.pool = w->d_pool;
+	d.off = w->d_off;
+	d.len = w->d_len;
+	d.shadow = w->d_shadow;
+	d.shadow_len = w->shadow_len;
+	d.shell_bits = w->d_shell_bits;
+	d.shell_col = w->d_shell_col;
+	d.shadow_w = w->shadow_w;
+	d.nchunks = w->nchunks;
+	d.root_bitw = (uint32_t)w->root_bitw;
+	for (int i = 0; i < 3; i++) d.max_bitw[i] = (uint32_t)w->max_bitw[i];
+	CK(cudaMemcpyAsync(w->d_set, &d, sizeof(d), cudaMemcpyHostToDevice, w->ctx->stream));
+	CK(cudaStreamSynchronize(w->ctx->stream));
+	return VP_OK;
+}
+
+VP_API int vp_world_upload(vp_world *w, const uint32_t *pool, uint64_t pool_words, const uint64_t *off,
+			   const uint32_t *len, const uint16_t *shadow, uint64_t shadow_len, uint32_t shadow_w)
+{
+	if (!w || !pool || !off || !len || (!shadow && shadow_len)) return VP_EINVAL;
+	const uint64_t N = 1ull << (3 * w->root_bitw);
+	/* validate and repack into a 16-byte aligned pool */
+	std::vector<uint64_t> noff(w->nchunks);
+	uint64_t total = 0;
+	for (uint32_t c = 0; c < w->nchunks; c++) {
+		if (off[c] + len[c] > pool_words) return VP_EINVAL;
+		int rc = validate_stream(pool + off[c], len[c], N);
+		if (rc) return rc;
+		noff[c] = total;
+		total += (len[c] + 3u) & ~3u;
+	}
+	total += 4; /* vector loads may read up to 3 words past a terminator */
+	std::vector<uint32_t> packed(total, 0u);
+	for (uint32_t c = 0; c < w->nchunks; c++)
+		memcpy(&packed[noff[c]], pool + off[c], (size_t)len[c] * sizeof(uint32_t));
+	CK(cudaSetDevice(w->ctx->device));
+	CK(cudaStreamSynchronize(w->ctx->stream));
+	dev_free(w->d_pool);
+	dev_free(w->d_shadow);
+	int rc;
+	if ((rc = dev_alloc(&w->d_pool, total))) return rc;
+	if ((rc = dev_alloc(&w->d_shadow, shadow_len + 8))) return rc;
+	cudaStream_t st = w->ctx->stream;
+	CK(cudaMemcpyAsync(w->d_pool, packed.data(), total * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+	CK(cudaMemcpyAsync(w->d_off, noff.data(), w->nchunks * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+	CK(cudaMemcpyAsync(w->d_len, len, w->nchunks * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+	CK(cudaMemsetAsync(w->d_shadow, 0, (shadow_len + 8) * sizeof(uint16_t), st));
+	if (shadow_len)
+		CK(cudaMemcpyAsync(w->d_shadow, shadow, shadow_len * sizeof(uint16_t), cudaMemcpyHostToDevice, st));
+	w->pool_words = total;
+	w->shadow_len = shadow_len;
+	w->shadow_w = shadow_w;
+	w->uploaded = true;
+	return upload_setdesc(w);
+}
+
+VP_API int vp_world_set_modes(vp_world *w, const uint8_t *make_mesh)
+{
+	if (!w) return VP_EINVAL;
+	for (uint32_t c = 0; c < w->nchunks; c++) w->modes[c] = make_mesh ? (make_mesh[c] ? 1 : 0) : 0;
+	w->items_dirty = true;
+	return VP_OK;
+}
+
+static int ensure_items(vp_world *w)
+{
+	if (!w->items_dirty) return VP_OK;
+	std::vector<WorkItem> it(w->nchunks);
+	for (uint32_t c = 0; c < w->nchunks; c++) {
+		it[c].set = 0;
+		it[c].chunk = c;
+		it[c].flags = w->modes[c] ? kItemMesh : 0u;
+		it[c].pad = 0;
+	}
+	CK(cudaMemcpyAsync(w->d_items, it.data(), it.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
+			   w->ctx->stream));
+	CK(cudaStreamSynchronize(w->ctx->stream));
+	w->items_dirty = false;
+	return VP_OK;
+}
+
+static int ensure_arenas(vp_world *w)
+{
+	/* first guess: 64 KiB of each output per chunk, at least 16 MiB */
+	for (int a = 0; a < 3; a++) {
+		if (w->d_arena[a]) continue;
+		uint64_t units = std::max<uint64_t>((uint64_t)w->nchunks * 4096u, 1u << 20);
+		cudaError_t e = cudaMalloc(&w->d_arena[a], units * 16u);
+		if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(arena)");
+		w->cap[a] = units;
+	}
+	return VP_OK;
+}
+
+static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
+{
+	vp_ctx *ctx = w->ctx;
+	cudaStream_t st = ctx->stream;
+	int rc;
+	if ((rc = ensure_items(w)) || (rc = ensure_arenas(w))) return rc;
+	CK(cudaMemsetAsync(w->d_cursors, 0, 3 * sizeof(unsigned long long), st));
+	CK(cudaMemsetAsync(w->d_queue, 0, sizeof(unsigned int), st));
+	GeoLaunch L;
+	memset(&L, 0, sizeof(L));
+	L.sets = w->d_set;
+	L.items = w->d_items;
+	L.n_items = w->nchunks;
+	L.shell_items = w->d_items;
+	L.n_shell = w->nchunks;
+	L.threads = 512;
+	L.outs = w->d_outs;
+	L.lod_max = lod_max;
+	Arena *ar[3] = {&L.svl, &L.vbo, &L.ibo};
+	for (int a = 0; a < 3; a++) {
+		ar[a]->base = w->d_arena[a];
+		ar[a]->cap_units = w->cap[a];
+		ar[a]->cursor = w->d_cursors + a;
+	}
+	if (flags & VP_REBUILD_PERSISTENT) {
+		const int per_sm = geometry_ctas_per_sm(w->root_bitw, (int)L.threads);
+		L.queue = w->d_queue;
+		L.ctas = (uint32_t)(ctx->sm_count * std::max(per_sm, 1));
+	}
+	cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+	if (ctx->timing) {
+		cudaEventCreate(&e0);
+		cudaEventCreate(&e1);
+		cudaEventCreate(&e2);
+		cudaEventRecord(e0, st);
+	}
+	/* shell pass */
+	L.run_shell = 1;
+	GeoLaunch Ls = L;
+	Ls.n_items = 0;
+	cudaError_t e = launch_geometry(w->root_bitw, Ls, st);
+	if (e != cudaSuccess) return cuda_fail(e, "shell launch");
+	if (ctx->timing) cudaEventRecord(e1, st);
+	GeoLaunch Lg = L;
+	Lg.run_shell = 0;
+	e = launch_geometry(w->root_bitw, Lg, st);
+	if (e != cudaSuccess) return cuda_fail(e, "geometry launch");
+	if (ctx->timing) {
+		cudaEventRecord(e2, st);
+		w->ev.push_back(e0);
+		w->ev.push_back(e1);
+		w->ev.push_back(e2);
+	}
+	w->launches += 2;
+	w->last_lod = lod_max;
+	w->last_flags = flags;
+	return VP_OK;
+}
+
+VP_API int vp_world_rebuild(vp_world *w, int lod_max, unsigned flags)
+{
+	if (!w || !w->uploaded) return VP_EINVAL;
+	if (lod_max < 0 || lod_max >= VP_MAX_LEVELS) return VP_EUNSUPPORTED;
+	CK(cudaSetDevice(w->ctx->device));
+	return enqueue_rebuild(w, lod_max, flags);
+}
+
+VP_API int vp_world_finish(vp_world *w)
+{
+	if (!w) return VP_EINVAL;
+	cudaStream_t st = w->ctx->stream;
+	for (int attempt = 0; attempt < 4; attempt++) {
+		unsigned long long cur[3];
+		CK(cudaMemcpyAsync(cur, w->d_cursors, sizeof(cur), cudaMemcpyDeviceToHost, st));
+		CK(cudaStreamSynchronize(st));
+		bool grow = false;
+		for (int a = 0; a < 3; a++) {
+			if (cur[a] <= w->cap[a]) continue;
+			grow = true;
+			uint64_t units = cur[a] + cur[a] / 4 + 1024;
+			dev_free(w->d_arena[a]);
+			cudaError_t e = cudaMalloc(&w->d_arena[a], units * 16u);
+			if (e != cudaSuccess) {
+				w->cap[a] = 0;
+				return cuda_fail(e, "cudaMalloc(arena growth)");
+			}
+			w->cap[a] = units;
+		}
+		if (!grow) return VP_OK;
+		int rc = enqueue_rebuild(w, w->last_lod, w->last_flags);
+		if (rc) return rc;
+	}
+	return VP_EOVERFLOW;
+}
+
+VP_API int vp_world_results(vp_world *w, vp_chunk_result *out, uint32_t n)
+{
+	static_assert(sizeof(vp_chunk_result) == sizeof(ChunkOut), "result record layout");
+	if (!w || !out || n > w->nchunks) return VP_EINVAL;
+	CK(cudaMemcpyAsync(out, w->d_outs, (size_t)n * sizeof(ChunkOut), cudaMemcpyDeviceToHost, w->ctx->stream));
+	CK(cudaStreamSynchronize(w->ctx->stream));
+	return VP_OK;
+}
+
+static int read_arena(vp_world *w, int a, uint64_t off_bytes, uint64_t nbytes, void *dst)
+{
+	if (!w || (!dst && nbytes)) return VP_EINVAL;
+	if (off_bytes + nbytes > w->cap[a] * 16u) return VP_EINVAL;
+	if (!nbytes) return VP_OK;
+	CK(cudaMemcpyAsync(dst, (const char *)w->d_arena[a] + off_bytes, nbytes, cudaMemcpyDeviceToHost,
+			   w->ctx->stream));
+	CK(cudaStreamSynchronize(w->ctx->stream));
+	return VP_OK;
+}
+
+VP_API int vp_world_read_svl(vp_world *w, uint64_t off, uint64_t n, int16_t *dst)
+{
+	return read_arena(w, 0, off * 2u, n * 2u, dst);
+}
+
+VP_API int vp_world_read_vbo(vp_world *w, uint64_t off, uint64_t n, int16_t *dst)
+{
+	return read_arena(w, 1, off * 2u, n * 2u, dst);
+}
+
+VP_API int vp_world_read_ibo(vp_world *w, uint64_t off, uint64_t n, uint32_t *dst)
+{
+	return read_arena(w, 2, off * 4u, n * 4u, dst);
+}
+
+VP_API int vp_world_kernel_ms(vp_world *w, double *shell_ms, double *geometry_ms, uint32_t *launches)
+{
+	if (!w) return VP_EINVAL;
+	CK(cudaStreamSynchronize(w->ctx->stream));
+	for (size_t i = 0; i + 2 < w->ev.size(); i += 3) {
+		float a = 0, b = 0;
+		cudaEventElapsedTime(&a, w->ev[i], w->ev[i + 1]);
+		cudaEventElapsedTime(&b, w->ev[i + 1], w->ev[i + 2]);
+		w->ms[0] += a;
+		w->ms[1] += b;
+	}
+	for (cudaEvent_t e : w->ev) cudaEventDestroy(e);
+	w->ev.clear();
+	if (shell_ms) *shell_ms = w->ms[0];
+	if (geometry_ms) *geometry_ms = w->ms[1];
+	if (launches) *launches = w->launches;
+	w->ms[0] = w->ms[1] = 0;
+	w->launches = 0;
+	return VP_OK;
+}
+
+} // extern "C"

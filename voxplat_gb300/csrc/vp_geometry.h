@@ -1,0 +1,28 @@
+/* vp_geometry.h — host-side launch interface of the geometry kernels. */
+#pragma once
+#include "vp_dev.cuh"
+
+namespace vp {
+
+struct GeoLaunch {
+	const SetDesc *sets;        /* device array */
+	const WorkItem *items;      /* device array: geometry work */
+	uint32_t n_items;
+	const WorkItem *shell_items;/* device array: chunks whose shell to write */
+	uint32_t n_shell;
+	int run_shell;
+	unsigned int *queue;        /* device counter for persistent CTAs, or NULL */
+	uint32_t ctas;              /* persistent grid size */
+	uint32_t threads;
+	ChunkOut *outs;
+	Arena svl, vbo, ibo;
+	int lod_max;
+};
+
+size_t geometry_smem_bytes(int root_bitw);
+size_t shell_words_per_chunk(int root_bitw);
+size_t shell_cols_per_chunk(int root_bitw);
+int geometry_ctas_per_sm(int root_bitw, int threads);
+cudaError_t launch_geometry(int root_bitw, const GeoLaunch &L, cudaStream_t st);
+
+} // namespace vp

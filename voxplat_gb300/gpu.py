@@ -1,0 +1,209 @@
+"""ctypes binding of libvoxgpu.so (include/voxgpu.h).
+
+`Context` and `DeviceWorld` mirror the C ABI one to one; `rebuild_world`
+is the convenience path used by tests and the benchmark.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+VP_OK = 0
+VP_MAX_LEVELS = 8
+VP_REBUILD_PERSISTENT = 1
+
+
+class VoxGpuError(RuntimeError):
+    pass
+
+
+class ChunkResult(ctypes.Structure):
+    _fields_ = [
+        ("svl_off", ctypes.c_uint64),
+        ("vbo_off", ctypes.c_uint64),
+        ("ibo_off", ctypes.c_uint64),
+        ("svl_items", ctypes.c_uint32 * VP_MAX_LEVELS),
+        ("svl_total", ctypes.c_uint32),
+        ("vbo_items", ctypes.c_uint32),
+        ("ibo_items", ctypes.c_uint32),
+        ("status", ctypes.c_uint32),
+    ]
+
+
+RESULT_DTYPE = np.dtype([
+    ("svl_off", np.uint64), ("vbo_off", np.uint64), ("ibo_off", np.uint64),
+    ("svl_items", np.uint32, (VP_MAX_LEVELS,)), ("svl_total", np.uint32),
+    ("vbo_items", np.uint32), ("ibo_items", np.uint32), ("status", np.uint32)])
+assert RESULT_DTYPE.itemsize == ctypes.sizeof(ChunkResult)
+
+_lib = None
+
+
+def lib_path():
+    return _build.LIBGPU
+
+
+def load(build_if_missing=True):
+    """Load libvoxgpu.so; raises VoxGpuError if it is missing or broken."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIBGPU
+    if build_if_missing and not os.path.exists(path):
+        _build.build_cuda()
+    if not os.path.exists(path):
+        raise VoxGpuError("libvoxgpu.so not built (run __graft_entry__.build())")
+    try:
+        lib = ctypes.CDLL(path)
+    except OSError as e:
+        raise VoxGpuError("cannot load %s: %s" % (path, e))
+    V, I, U32, U64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64
+    PV = ctypes.POINTER(V)
+    sig = {
+        "vp_strerror": (ctypes.c_char_p, [I]),
+        "vp_last_cuda_error": (ctypes.c_char_p, []),
+        "vp_ctx_create": (I, [I, PV]),
+        "vp_ctx_destroy": (None, [V]),
+        "vp_ctx_stream": (V, [V]),
+        "vp_ctx_sync": (I, [V]),
+        "vp_ctx_set_timing": (I, [V, I]),
+        "vp_world_create": (I, [V, I, V, PV]),
+        "vp_world_destroy": (None, [V]),
+        "vp_world_upload": (I, [V, V, U64, V, V, V, U64, U32]),
+        "vp_world_set_modes": (I, [V, V]),
+        "vp_world_rebuild": (I, [V, I, ctypes.c_uint]),
+        "vp_world_finish": (I, [V]),
+        "vp_world_results": (I, [V, V, U32]),
+        "vp_world_read_svl": (I, [V, U64, U64, V]),
+        "vp_world_read_vbo": (I, [V, U64, U64, V]),
+        "vp_world_read_ibo": (I, [V, U64, U64, V]),
+        "vp_world_kernel_ms": (I, [V, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                   ctypes.POINTER(U32)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc, what=""):
+    if rc != VP_OK:
+        lib = load()
+        raise VoxGpuError("%s failed: %s (%d) %s" % (
+            what, lib.vp_strerror(rc).decode(), rc, lib.vp_last_cuda_error().decode()))
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+class Context:
+    def __init__(self, device=0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        check(self.lib.vp_ctx_create(device, ctypes.byref(h)), "vp_ctx_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.vp_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self):
+        return self.lib.vp_ctx_stream(self.h)
+
+    def sync(self):
+        check(self.lib.vp_ctx_sync(self.h), "vp_ctx_sync")
+
+    def set_timing(self, on):
+        check(self.lib.vp_ctx_set_timing(self.h, 1 if on else 0), "vp_ctx_set_timing")
+
+
+class DeviceWorld:
+    """A device-resident world (one reference ChunkSet)."""
+
+    def __init__(self, ctx, world):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.world = world
+        self.nchunks = world.nchunks
+        h = ctypes.c_void_p()
+        mb = (ctypes.c_int * 3)(*world.max_bitw)
+        check(self.lib.vp_world_create(ctx.h, world.root_bitw, mb, ctypes.byref(h)), "vp_world_create")
+        self.h = h
+        self.upload(world)
+
+    def upload(self, world):
+        check(self.lib.vp_world_upload(self.h, _p(world.pool), len(world.pool), _p(world.off), _p(world.len),
+                                       _p(world.shadow), len(world.shadow), world.shadow_w), "vp_world_upload")
+
+    def close(self):
+        if self.h:
+            self.lib.vp_world_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_modes(self, make_mesh):
+        if make_mesh is None:
+            check(self.lib.vp_world_set_modes(self.h, None), "vp_world_set_modes")
+        else:
+            m = np.ascontiguousarray(make_mesh, dtype=np.uint8)
+            assert len(m) == self.nchunks
+            check(self.lib.vp_world_set_modes(self.h, _p(m)), "vp_world_set_modes")
+
+    def rebuild(self, lod_max=4, persistent=True):
+        flags = VP_REBUILD_PERSISTENT if persistent else 0
+        check(self.lib.vp_world_rebuild(self.h, lod_max, flags), "vp_world_rebuild")
+
+    def finish(self):
+        check(self.lib.vp_world_finish(self.h), "vp_world_finish")
+
+    def results(self):
+        out = np.zeros(self.nchunks, RESULT_DTYPE)
+        check(self.lib.vp_world_results(self.h, _p(out), self.nchunks), "vp_world_results")
+        return out
+
+    def read_svl(self, off, n):
+        out = np.zeros(int(n), np.int16)
+        check(self.lib.vp_world_read_svl(self.h, int(off), int(n), _p(out)), "vp_world_read_svl")
+        return out
+
+    def read_vbo(self, off, n):
+        out = np.zeros(int(n), np.int16)
+        check(self.lib.vp_world_read_vbo(self.h, int(off), int(n), _p(out)), "vp_world_read_vbo")
+        return out
+
+    def read_ibo(self, off, n):
+        out = np.zeros(int(n), np.uint32)
+        check(self.lib.vp_world_read_ibo(self.h, int(off), int(n), _p(out)), "vp_world_read_ibo")
+        return out
+
+    def kernel_ms(self):
+        a, b, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint32()
+        check(self.lib.vp_world_kernel_ms(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)),
+              "vp_world_kernel_ms")
+        return a.value, b.value, n.value
+
+    def chunk_splats(self, res, c):
+        r = res[c]
+        return self.read_svl(r["svl_off"], r["svl_total"]), r["svl_items"].copy()
+
+    def chunk_mesh(self, res, c):
+        r = res[c]
+        return self.read_vbo(r["vbo_off"], r["vbo_items"]), self.read_ibo(r["ibo_off"], r["ibo_items"])
