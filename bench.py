@@ -1,0 +1,336 @@
+"""Benchmark: full-world geometry rebuild on one GB300.
+
+Workload (one "step"): every chunk of a 2048x256x2048 world of 64^3 chunks
+(32x4x32 = 4096 chunks), terrain + caves, RLE-resident in HBM, goes through
+decode -> exposure cull -> LOD 0..4 -> splat emission, or -> quad mesh for
+chunks whose centre lies within 512 voxels of the camera (the reference's
+near/far rule, src/game.c:612-618). Metric: 64^3 chunks per second.
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
+
+Under torchrun (N > 1) every rank rebuilds its own replica world (the path
+has no exchange step); `value` is the chunks of all ranks over the slowest
+rank's time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "64³ chunks/s (RLE→cull→LOD→emit) batched vs plain on 1 GB300; edit→mesh p99 ms"
+SEED = 2024
+LOD_MAX = 4
+CAMERA = (1024.0, 160.0, 1024.0)
+MESH_RADIUS = 512.0
+L2_FLUSH_BYTES = 512 << 20
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def make_world():
+    from voxplat_gb300 import worldgen as wg
+    return wg.terrain(wg.TERRAIN_CAVES, 6, (5, 2, 5), seed=SEED)
+
+
+def mesh_modes(world):
+    R = world.R
+    n = world.nchunks
+    c = np.arange(n)
+    bx, by, _ = world.max_bitw
+    xs = (c & ((1 << bx) - 1)) * R + R // 2
+    ys = ((c >> bx) & ((1 << by) - 1)) * R + R // 2
+    zs = (c >> (bx + by)) * R + R // 2
+    d = np.sqrt((xs - CAMERA[0]) ** 2 + (ys - CAMERA[1]) ** 2 + (zs - CAMERA[2]) ** 2)
+    return (d < MESH_RADIUS).astype(np.uint8)
+
+
+def workload_config(world, modes):
+    return {
+        "workload": "2048x256x2048 world, 32x4x32 chunks of 64^3, terrain+caves (seed %d), RLE-resident; "
+                    "decode+cull+LOD0..4+splats, near chunks (<512 voxels from camera) meshed" % SEED,
+        "chunks": int(world.nchunks),
+        "chunk_size": int(world.R),
+        "lod_max": LOD_MAX,
+        "mesh_chunks": int(modes.sum()),
+        "rle_mb": round(world.rle_bytes() / 1e6, 2),
+        "l2": "flushed between timed steps (512 MiB write)",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[4 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return rank, ws, dist
+
+
+def cpu_baseline(world, modes, budget_s=12.0, threads=None):
+    """The oracle (C restatement of the reference mesher) on a bounded sample
+    of the workload's chunks, OpenMP over all host cores."""
+    from oracle.bindings import OracleWorld
+    threads = threads or os.cpu_count()
+    o = OracleWorld(world)
+    rng = np.random.default_rng(1)
+    order = rng.permutation(world.nchunks).astype(np.uint32)
+    n = 256
+    t0 = time.perf_counter()
+    o.rebuild(order[:n], modes, LOD_MAX, threads)
+    dt = time.perf_counter() - t0
+    # grow the sample to fill the budget, then time it once more
+    n = int(min(world.nchunks, max(n, n * budget_s / max(dt, 1e-3) / 2)))
+    t0 = time.perf_counter()
+    o.rebuild(order[:n], modes, LOD_MAX, threads)
+    dt = time.perf_counter() - t0
+    return {"value": round(n / dt, 1), "unit": "chunks/s", "cores": threads, "kind": "port",
+            "sample": "%d of the %d chunks (random, seed 1), cold decode, same modes/LOD" % (n, world.nchunks)}
+
+
+def algorithmic_bytes(world, res):
+    """Per rebuild: RLE read + splat/mesh output + shadow map read once."""
+    rle = int(world.len.astype(np.int64).sum()) * 4
+    out = int(res["svl_total"].astype(np.int64).sum()) * 2 + int(res["vbo_items"].astype(np.int64).sum()) * 2 \
+        + int(res["ibo_items"].astype(np.int64).sum()) * 4
+    shadow = world.shadow_w * world.shadow_z * 2
+    return rle + out + shadow, rle, out, shadow
+
+
+def run_ours(args):
+    import torch
+    from voxplat_gb300 import gpu
+    rank, ws, dist = dist_setup()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    world = make_world()
+    modes = mesh_modes(world)
+    ctx = gpu.Context(dev)
+    dw = gpu.DeviceWorld(ctx, world)
+    dw.set_modes(modes)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda:%d" % dev)
+    for _ in range(max(args.warmup, 3)):
+        dw.rebuild(LOD_MAX)
+        dw.finish()
+    res = dw.results()
+    assert (res["status"] == 0).all()
+    ctx.set_timing(True)
+    dw.kernel_ms()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                starts[k].record(stream)
+            dw.rebuild(LOD_MAX)
+            with torch.cuda.stream(stream):
+                ends[k].record(stream)
+        ctx.sync()
+        torch.cuda.synchronize()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    shell_ms, geo_ms, launches = dw.kernel_ms()
+    ctx.set_timing(False)
+    t_ms = float(np.sum(step_ms))
+    if dist:
+        tt = torch.tensor([t_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    chunks = world.nchunks * args.steps * ws
+    value = chunks / (t_ms / 1e3)
+    ab, rle_b, out_b, sh_b = algorithmic_bytes(world, res)
+    geo_avg_ms = geo_ms / args.steps
+    peak, peak_kind = peaks()
+    achieved = ab / (geo_avg_ms / 1e3) / 1e9
+    # end to end through the C ABI with host buffers
+    e2e_t = []
+    h2d = world.pool.nbytes + world.off.nbytes + world.len.nbytes + world.shadow.nbytes + modes.nbytes
+    d2h = 0
+    for k in range(max(2, min(args.steps, 5))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dw.upload(world)
+        dw.set_modes(modes)
+        dw.rebuild(LOD_MAX)
+        dw.finish()
+        r = dw.results()
+        tot_svl = int(np.max(r["svl_off"] + r["svl_total"])) if len(r) else 0
+        tot_vbo = int(np.max(r["vbo_off"] + r["vbo_items"])) if len(r) else 0
+        tot_ibo = int(np.max(r["ibo_off"] + r["ibo_items"])) if len(r) else 0
+        a = dw.read_svl(0, tot_svl)
+        b = dw.read_vbo(0, tot_vbo)
+        c = dw.read_ibo(0, tot_ibo)
+        e2e_t.append(time.perf_counter() - t0)
+        d2h = r.nbytes + a.nbytes + b.nbytes + c.nbytes
+    e2e_value = world.nchunks / float(np.median(e2e_t))
+    out = {
+        "metric": METRIC,
+        "value": round(value, 1),
+        "unit": "chunks/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(t_ms / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u8",
+        "data": "synthetic (seeded integer-hash terrain + caves; no dataset)",
+        "config": workload_config(world, modes),
+        "voxels_per_s": round(value * world.R ** 3, 1),
+        "kernel_ms": {"shell": round(shell_ms / args.steps, 4), "geometry": round(geo_avg_ms, 4)},
+        "e2e": {"value": round(e2e_value, 1), "unit": "chunks/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h),
+                "path": "vp_world_upload + vp_world_rebuild + vp_world_finish + results/arena readback"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None,
+                     "kernel": "k_geometry<6>", "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": int(ab),
+                     "bytes_split": {"rle_in": rle_b, "geometry_out": out_b, "shadow_map": sh_b}},
+        "gpu_launches": int(launches),
+    }
+    if rank == 0:
+        out["clocks"] = clk.summary()
+        out["cpu_baseline"] = cpu_baseline(world, modes)
+        print(json.dumps(out), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle.bindings import OracleWorld
+    threads = os.cpu_count()
+    world = make_world()
+    modes = mesh_modes(world)
+    o = OracleWorld(world)
+    rng = np.random.default_rng(1)
+    order = rng.permutation(world.nchunks).astype(np.uint32)
+    n = 768
+    for _ in range(max(args.warmup, 1)):
+        o.rebuild(order[:n], modes, LOD_MAX, threads)
+    ts = []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        o.rebuild(order[:n], modes, LOD_MAX, threads)
+        ts.append(time.perf_counter() - t0)
+    t = float(np.sum(ts))
+    value = n * args.steps / t
+    sample = "%d of the %d chunks per step (random, seed 1), cold decode" % (n, world.nchunks)
+    out = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": round(value, 1),
+        "unit": "chunks/s",
+        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(t * 1e3 / args.steps, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u8",
+        "data": "synthetic (seeded integer-hash terrain + caves; no dataset)",
+        "config": workload_config(world, modes),
+        "cpu_baseline": {"value": round(value, 1), "unit": "chunks/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 1), "unit": "chunks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    import __graft_entry__
+    __graft_entry__.build()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

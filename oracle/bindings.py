@@ -41,6 +41,9 @@ def vpo_lib():
         lib.vpo_rle_decode.argtypes = [V, V, ctypes.c_uint32]
         lib.vpo_edit_sphere.restype = ctypes.c_uint32
         lib.vpo_edit_sphere.argtypes = [V, V, ctypes.c_uint32, ctypes.c_uint8, V]
+        lib.vpo_world_drop_voxels.argtypes = [V]
+        lib.vpo_rebuild.restype = ctypes.c_uint64
+        lib.vpo_rebuild.argtypes = [V, V, ctypes.c_uint32, V, ctypes.c_int, ctypes.c_int]
         lib.vpo_group_node.restype = ctypes.c_uint64
         lib.vpo_group_node.argtypes = [V, ctypes.c_int, V, V, V, V]
         _vpo = lib
@@ -130,6 +133,15 @@ class OracleWorld(_Base):
 
     def _mesh(self, c, vbo, nv, ibo, ni):
         self.lib.vpo_make_mesh(self.h, c, _vp(vbo), _vp(nv), _vp(ibo), _vp(ni))
+
+    def rebuild(self, chunks, make_mesh, lod_max, nthreads, cold=True):
+        """Timed CPU baseline: reference per-chunk work over `chunks`."""
+        chunks = np.ascontiguousarray(chunks, np.uint32)
+        mm = None if make_mesh is None else np.ascontiguousarray(make_mesh, np.uint8)
+        if cold:
+            self.lib.vpo_world_drop_voxels(self.h)
+        return self.lib.vpo_rebuild(self.h, _vp(chunks), len(chunks), _vp(mm) if mm is not None else None,
+                                    lod_max, nthreads)
 
     def mask(self, c):
         m = np.zeros((self.R + 1) ** 3, np.uint8)

@@ -522,3 +522,69 @@ uint64_t vpo_group_node(const vpo_world *w, int lod, const uint32_t node[3], int
 			}
 	return total;
 }
+
+/* Drop every decoded chunk (the reference compresses idle chunks again,
+ * src/chunkset.c:298-306); the next access decodes from RLE. */
+void vpo_world_drop_voxels(vpo_world *w)
+{
+	for (uint32_t c = 0; c < w->nchunks; c++) {
+		free(w->vox[c]);
+		w->vox[c] = NULL;
+	}
+}
+
+/* chunkset_manage's per-chunk work (src/chunkset.c:251-505) for a list of
+ * chunks, OpenMP-parallel over chunks like the reference (there: 4 threads,
+ * 8 chunks per 5 ms tick; here: `nthreads` threads, no throttles). Each
+ * chunk is opened (decoded on first use), meshed or masked + splatted, and
+ * its output copied into an exact-size buffer, as the reference publishes
+ * it. Returns the total number of output bytes produced. */
+uint64_t vpo_rebuild(vpo_world *w, const uint32_t *chunks, uint32_t n, const uint8_t *make_mesh, int lod_max,
+		     int nthreads)
+{
+	const size_t R = (size_t)w->R, S3 = (R + 1) * (R + 1) * (R + 1);
+	size_t geom_cap = 0;
+	for (int l = 0; l <= lod_max; l++) geom_cap += 4 * (((R >> l) + 1) * ((R >> l) + 1) * ((R >> l) + 1));
+	uint64_t total = 0;
+#pragma omp parallel num_threads(nthreads) reduction(+ : total)
+	{
+		int16_t *geom = NULL;
+		int16_t *vbo = NULL;
+		uint32_t *ibo = NULL;
+		uint8_t *mask = (uint8_t *)malloc(S3), *work = (uint8_t *)malloc(S3);
+#pragma omp for schedule(dynamic, 1)
+		for (uint32_t k = 0; k < n; k++) {
+			uint32_t c = chunks[k];
+			vpo_world_voxels(w, c);
+			if (make_mesh && make_mesh[c]) {
+				if (!vbo) {
+					vbo = (int16_t *)malloc(3 * R * R * R * 16 * sizeof(int16_t));
+					ibo = (uint32_t *)malloc(3 * R * R * R * 6 * sizeof(uint32_t));
+				}
+				uint32_t nv = 0, ni = 0;
+				vpo_make_mesh(w, c, vbo, &nv, ibo, &ni);
+				int16_t *pv = (int16_t *)malloc((size_t)nv * sizeof(int16_t) + 1);
+				uint32_t *pi = (uint32_t *)malloc((size_t)ni * sizeof(uint32_t) + 1);
+				memcpy(pv, vbo, (size_t)nv * sizeof(int16_t));
+				memcpy(pi, ibo, (size_t)ni * sizeof(uint32_t));
+				total += (uint64_t)nv * 2 + (uint64_t)ni * 4;
+				free(pv);
+				free(pi);
+			} else {
+				if (!geom) geom = (int16_t *)malloc(geom_cap * sizeof(int16_t));
+				uint32_t items[VPO_MAX_LEVELS];
+				uint32_t t = vpo_chunk_splats(w, c, lod_max, geom, items, mask, work);
+				int16_t *ps = (int16_t *)malloc((size_t)t * sizeof(int16_t) + 1);
+				memcpy(ps, geom, (size_t)t * sizeof(int16_t));
+				total += (uint64_t)t * 2;
+				free(ps);
+			}
+		}
+		free(geom);
+		free(vbo);
+		free(ibo);
+		free(mask);
+		free(work);
+	}
+	return total;
+}

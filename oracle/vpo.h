@@ -23,6 +23,8 @@
 #ifndef VPO_H
 #define VPO_H
 
+#define VPO_MAX_LEVELS 8
+
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -87,6 +89,12 @@ uint32_t vpo_edit_sphere(vpo_world *w, const int32_t ws[3], uint32_t radius, uin
  * Returns int16 items written. */
 uint64_t vpo_group_node(const vpo_world *w, int lod, const uint32_t node[3],
 			int16_t *const *svl, const uint32_t *const *svl_items, int16_t *out);
+
+/* Timed CPU baseline: the reference's per-chunk mesher work for `chunks`,
+ * OpenMP over chunks; returns output bytes. */
+void vpo_world_drop_voxels(vpo_world *w);
+uint64_t vpo_rebuild(vpo_world *w, const uint32_t *chunks, uint32_t n, const uint8_t *make_mesh, int lod_max,
+		     int nthreads);
 
 #ifdef __cplusplus
 }
