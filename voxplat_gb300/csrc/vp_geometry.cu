@@ -45,27 +45,29 @@ struct Geo {
 		return t;
 	}
 	static constexpr size_t a16(size_t v) { return (v + 15) & ~(size_t)15; }
-	/* shared memory carve, byte offsets (every region 16-byte aligned) */
+	/* shared memory carve, byte offsets (every region 16-byte aligned):
+	 * 64^3 chunks need ~98 KB, so two CTAs share an SM */
 	static constexpr size_t o_occ = 0;
 	static constexpr size_t o_rs = a16(o_occ + sizeof(uint64_t) * H * H);
-	static constexpr size_t o_e0 = a16(o_rs + sizeof(uint64_t) * RR);
-	static constexpr size_t o_e0p = a16(o_e0 + sizeof(uint64_t) * RR);
-	static constexpr size_t o_lv = a16(o_e0p + sizeof(uint64_t) * 3 * R);
-	static constexpr size_t o_rank = a16(o_lv + sizeof(uint64_t) * lv_words());
-	static constexpr size_t o_rowoff = a16(o_rank + sizeof(uint32_t) * RR);
-	static constexpr size_t o_xlo = a16(o_rowoff + sizeof(uint32_t) * S * S);
-	static constexpr size_t o_xhi = a16(o_xlo + H * H);
-	static constexpr size_t o_col = a16(o_xhi + H * H);
-	static constexpr size_t o_tmp = a16(o_col + 3 * RR);
-	static constexpr size_t bytes = a16(o_tmp + sizeof(uint32_t) * 64);
+	static constexpr size_t o_rank = a16(o_rs + sizeof(uint64_t) * RR);
+	static constexpr size_t o_lv = a16(o_rank + sizeof(uint32_t) * RR);
+	static constexpr size_t o_xrow = a16(o_lv + sizeof(uint64_t) * lv_words());
+	static constexpr size_t o_xedge = a16(o_xrow + sizeof(uint64_t) * 2 * H);
+	static constexpr size_t o_tmp = a16(o_xedge + 4 * H);
+	static constexpr size_t o_wb = a16(o_tmp + sizeof(uint32_t) * 64);
+	static constexpr size_t o_nbr = a16(o_wb + sizeof(uint32_t) * kMaxLevels * 16);
+	static constexpr size_t bytes = a16(o_nbr + sizeof(int32_t) * 28);
 	static constexpr size_t shell_words = 6 * R;   /* u64 per chunk */
 	static constexpr size_t shell_cols = 3 * RR;   /* bytes per chunk */
 };
 
 struct Smem {
-	uint64_t *occ, *rs, *e0, *e0p, *lv;
-	uint32_t *rank, *rowoff, *tmp;
-	uint8_t *xlo, *xhi, *col;
+	uint64_t *occ, *rs, *lv;
+	uint32_t *rank, *tmp;
+	uint32_t *wb;    /* [level][warp] emission bases */
+	uint64_t *xrow;  /* [side][z+1]: x = -1 (side 0) / x = R (side 1), bits over y */
+	uint8_t *xedge;  /* [side*2 + (y == R)][z+1]: the y = -1 / y = R corners */
+	int32_t *nbr;    /* 27 neighbour chunk indices, -1 = air (outside or null) */
 };
 
 template <int RB>
@@ -75,15 +77,13 @@ __device__ __forceinline__ Smem carve(uint8_t *base)
 	Smem s;
 	s.occ = (uint64_t *)(base + G::o_occ);
 	s.rs = (uint64_t *)(base + G::o_rs);
-	s.e0 = (uint64_t *)(base + G::o_e0);
-	s.e0p = (uint64_t *)(base + G::o_e0p);
-	s.lv = (uint64_t *)(base + G::o_lv);
 	s.rank = (uint32_t *)(base + G::o_rank);
-	s.rowoff = (uint32_t *)(base + G::o_rowoff);
-	s.xlo = base + G::o_xlo;
-	s.xhi = base + G::o_xhi;
-	s.col = base + G::o_col;
+	s.lv = (uint64_t *)(base + G::o_lv);
+	s.xrow = (uint64_t *)(base + G::o_xrow);
+	s.xedge = base + G::o_xedge;
 	s.tmp = (uint32_t *)(base + G::o_tmp);
+	s.wb = (uint32_t *)(base + G::o_wb);
+	s.nbr = (int32_t *)(base + G::o_nbr);
 	return s;
 }
 
@@ -252,7 +252,7 @@ __device__ __forceinline__ uint32_t colour_at(const uint32_t *__restrict__ s, co
 /* ------------------------------------------------------------------ */
 
 template <int RB>
-__global__ void __launch_bounds__(512) k_shell(const SetDesc *__restrict__ sets, const WorkItem *__restrict__ items,
+__global__ void __launch_bounds__(512, 2) k_shell(const SetDesc *__restrict__ sets, const WorkItem *__restrict__ items,
 					       uint32_t nitems)
 {
 	using G = Geo<RB>;
@@ -310,13 +310,29 @@ __global__ void __launch_bounds__(512) k_shell(const SetDesc *__restrict__ sets,
 /* Geometry pass                                                       */
 /* ------------------------------------------------------------------ */
 
-/* Occupancy row (bits over x) of the neighbour-local row (ly, lz) of chunk
- * nc, taken from its shell. */
+__device__ __forceinline__ int nbr_slot(int dx, int dy, int dz) { return (dx + 1) + 3 * (dy + 1) + 9 * (dz + 1); }
+
+/* Fill the 27-entry neighbour table: chunk index, or -1 where the neighbour
+ * is outside the world or all air (its shell was not written). */
+__device__ __forceinline__ void load_neighbours(const SetDesc &S, const uint32_t cv[3], const Smem &m, uint32_t N)
+{
+	if (threadIdx.x < 27) {
+		const int t = threadIdx.x;
+		const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
+		int64_t nc = neighbour(S, cv, dx, dy, dz);
+		if (nc >= 0 && chunk_is_null(S, (uint32_t)nc, N)) nc = -1;
+		m.nbr[t] = (int32_t)nc;
+	}
+	__syncthreads();
+}
+
+/* Occupancy row (bits over x) of neighbour-local row (ly, lz), from the
+ * neighbour's shell; the row lies on one of its y or z boundary planes. */
 template <int RB>
-__device__ __forceinline__ uint64_t shell_row(const SetDesc &S, int64_t nc, int ly, int lz, uint32_t N)
+__device__ __forceinline__ uint64_t shell_row(const SetDesc &S, int32_t nc, int ly, int lz)
 {
 	constexpr int R = Geo<RB>::R;
-	if (nc < 0 || chunk_is_null(S, (uint32_t)nc, N)) return 0ull;
+	if (nc < 0) return 0ull;
 	const uint64_t *b = S.shell_bits + (size_t)nc * Geo<RB>::shell_words;
 	if (ly == 0) return b[kPY0 * R + lz];
 	if (ly == R - 1) return b[kPY1 * R + lz];
@@ -324,27 +340,23 @@ __device__ __forceinline__ uint64_t shell_row(const SetDesc &S, int64_t nc, int 
 	return b[kPZ1 * R + ly];
 }
 
-/* One occupancy bit (x = 0 or R-1 side plane) of chunk nc. */
+/* Row lz of the neighbour's x = 0 (lx == 0) or x = R-1 plane: bits over y. */
 template <int RB>
-__device__ __forceinline__ uint32_t shell_xbit(const SetDesc &S, int64_t nc, int lx, int ly, int lz, uint32_t N)
+__device__ __forceinline__ uint64_t shell_xrow(const SetDesc &S, int32_t nc, int lx, int lz)
 {
 	constexpr int R = Geo<RB>::R;
-	if (nc < 0 || chunk_is_null(S, (uint32_t)nc, N)) return 0u;
+	if (nc < 0) return 0ull;
 	const uint64_t *b = S.shell_bits + (size_t)nc * Geo<RB>::shell_words;
-	const uint64_t w = (lx == 0) ? b[kPX0 * R + lz] : b[kPX1 * R + lz];
-	return (uint32_t)((w >> ly) & 1ull);
+	return (lx == 0) ? b[kPX0 * R + lz] : b[kPX1 * R + lz];
 }
 
 template <int RB>
-__device__ void load_halo(const SetDesc &S, const uint32_t cv[3], const Smem &m, bool need_minus)
+__device__ void load_halo(const SetDesc &S, const Smem &m)
 {
 	using G = Geo<RB>;
-	constexpr int R = G::R, H = G::H, RR = G::RR;
-	const uint32_t N = (uint32_t)R * R * R;
-	/* halo rows: y in {-1, R} for z in [-1, R], and z in {-1, R} for y in
-	 * [0, R). Minus-side rows are only needed by the mesh path. */
-	const int nrow = 2 * H + 2 * R;
-	for (int i = threadIdx.x; i < nrow; i += blockDim.x) {
+	constexpr int R = G::R, H = G::H;
+	/* halo rows: y in {-1, R} for z in [-1, R], and z in {-1, R} for y in [0, R) */
+	for (int i = threadIdx.x; i < 2 * H + 2 * R; i += blockDim.x) {
 		int y, z;
 		if (i < 2 * H) {
 			y = (i < H) ? -1 : R;
@@ -356,86 +368,100 @@ __device__ void load_halo(const SetDesc &S, const uint32_t cv[3], const Smem &m,
 		}
 		const int dy = y < 0 ? -1 : (y >= R ? 1 : 0);
 		const int dz = z < 0 ? -1 : (z >= R ? 1 : 0);
-		uint64_t v = 0;
-		if (need_minus || (dy >= 0 && dz >= 0)) {
-			const int64_t nc = neighbour(S, cv, 0, dy, dz);
-			v = shell_row<RB>(S, nc, y - dy * R, z - dz * R, N);
-		}
-		m.occ[hidx<RB>(y, z)] = v;
+		m.occ[hidx<RB>(y, z)] = shell_row<RB>(S, m.nbr[nbr_slot(0, dy, dz)], y - dy * R, z - dz * R);
 	}
-	/* x = -1 and x = R columns for (y, z) in [-1, R]^2 */
-	for (int i = threadIdx.x; i < 2 * H * H; i += blockDim.x) {
-		const int side = i / (H * H), k = i % (H * H);
-		const int y = (k % H) - 1, z = (k / H) - 1;
+	/* x = -1 / x = R columns: one word over y per z, plus the y = -1 and
+	 * y = R corners from the diagonal neighbours */
+	for (int i = threadIdx.x; i < 2 * H; i += blockDim.x) {
+		const int side = i / H, z = (i % H) - 1;
 		const int dx = side ? 1 : -1;
-		const int dy = y < 0 ? -1 : (y >= R ? 1 : 0);
+		const int lx = side ? 0 : R - 1;
 		const int dz = z < 0 ? -1 : (z >= R ? 1 : 0);
-		uint32_t v = 0;
-		if (need_minus || (dx > 0 && dy >= 0 && dz >= 0)) {
-			const int64_t nc = neighbour(S, cv, dx, dy, dz);
-			v = shell_xbit<RB>(S, nc, side ? 0 : R - 1, y - dy * R, z - dz * R, N);
-		}
-		(side ? m.xhi : m.xlo)[k] = (uint8_t)v;
-	}
-	/* colours of the +x / +y / +z neighbour cells (their low planes) */
-	const int64_t nb[3] = {neighbour(S, cv, 1, 0, 0), neighbour(S, cv, 0, 1, 0), neighbour(S, cv, 0, 0, 1)};
-	for (int a = 0; a < 3; a++) {
-		uint4 *dst = (uint4 *)(m.col + a * RR);
-		const bool live = nb[a] >= 0 && !chunk_is_null(S, (uint32_t)nb[a], N);
-		const uint4 *src = live ? (const uint4 *)(S.shell_col + (size_t)nb[a] * G::shell_cols + (size_t)a * RR) : nullptr;
-		for (int i = threadIdx.x; i < RR / 16; i += blockDim.x)
-			dst[i] = live ? __ldg(src + i) : make_uint4(0, 0, 0, 0);
+		const int lz = z - dz * R;
+		m.xrow[side * H + z + 1] = shell_xrow<RB>(S, m.nbr[nbr_slot(dx, 0, dz)], lx, lz);
+		const uint64_t ym = shell_xrow<RB>(S, m.nbr[nbr_slot(dx, -1, dz)], lx, lz);
+		const uint64_t yp = shell_xrow<RB>(S, m.nbr[nbr_slot(dx, 1, dz)], lx, lz);
+		m.xedge[(side * 2 + 0) * H + z + 1] = (uint8_t)((ym >> (R - 1)) & 1ull);
+		m.xedge[(side * 2 + 1) * H + z + 1] = (uint8_t)(yp & 1ull);
 	}
 	__syncthreads();
+}
+
+/* The x = R column bit at (y, z), y and z in [0, R). */
+template <int RB>
+__device__ __forceinline__ uint64_t xhi_bit(const Smem &m, int y, int z)
+{
+	return (m.xrow[Geo<RB>::H + z + 1] >> y) & 1ull;
 }
 
 template <int RB>
 __device__ __forceinline__ uint32_t occ_at(const Smem &m, int x, int y, int z)
 {
-	constexpr int R = Geo<RB>::R;
-	const int k = hidx<RB>(y, z);
-	if (x < 0) return m.xlo[k];
-	if (x >= R) return m.xhi[k];
-	return (uint32_t)((m.occ[k] >> x) & 1ull);
+	constexpr int R = Geo<RB>::R, H = Geo<RB>::H;
+	if (x < 0 || x >= R) {
+		const int side = x >= R;
+		if (y < 0) return m.xedge[(side * 2) * H + z + 1];
+		if (y >= R) return m.xedge[(side * 2 + 1) * H + z + 1];
+		return (uint32_t)((m.xrow[side * H + z + 1] >> y) & 1ull);
+	}
+	return (uint32_t)((m.occ[hidx<RB>(y, z)] >> x) & 1ull);
 }
 
-/* L0 mask row (y, z) in [0, R]^2: bits x in [0, R) plus the x = R cell. */
+/* L0 mask row (y, z) in [0, R]^2 (src/chunkset/mesher.c:421-446 restated
+ * per bit): a solid voxel is in the mask when any +axis neighbour (the
+ * +chunk's voxel at coordinate R) is air, or a -axis neighbour inside the
+ * chunk is air; a cell at coordinate R is in the mask when the +chunk's
+ * voxel is solid and ours air. Bits x in [0, R); *xr = the x = R cell. */
 template <int RB>
 __device__ __forceinline__ uint64_t e0_row(const Smem &m, int y, int z, uint32_t &xr)
 {
-	constexpr int R = Geo<RB>::R;
+	using G = Geo<RB>;
+	constexpr int R = G::R;
 	xr = 0;
 	if (y < R && z < R) {
-		xr = (uint32_t)((m.e0p[z] >> y) & 1ull);
-		return m.e0[(z << RB) | y];
+		const uint64_t o = m.occ[hidx<RB>(y, z)];
+		const uint64_t xh = xhi_bit<RB>(m, y, z);
+		xr = (uint32_t)(xh & ~(o >> (R - 1)) & 1ull);
+		const uint64_t xp = (o >> 1) | (xh << (R - 1));
+		const uint64_t xm = ((o << 1) | 1ull) & G::MASK;
+		const uint64_t yp = m.occ[hidx<RB>(y + 1, z)];
+		const uint64_t ym = y ? m.occ[hidx<RB>(y - 1, z)] : G::MASK;
+		const uint64_t zp = m.occ[hidx<RB>(y, z + 1)];
+		const uint64_t zm = z ? m.occ[hidx<RB>(y, z - 1)] : G::MASK;
+		return o & ~(xp & xm & yp & ym & zp & zm);
 	}
-	if (y == R && z < R) return m.e0p[R + z];
-	if (z == R && y < R) return m.e0p[2 * R + y];
+	if (y == R && z < R) return m.occ[hidx<RB>(R, z)] & ~m.occ[hidx<RB>(R - 1, z)];
+	if (z == R && y < R) return m.occ[hidx<RB>(y, R)] & ~m.occ[hidx<RB>(y, R - 1)];
 	return 0ull;
 }
 
+/* Level-l mask row (y, z); level 0 includes the x = R cell in *xr. */
 template <int RB>
-__device__ __forceinline__ uint32_t level_bit(const Smem &m, const int *lvoff, int l, int x, int y, int z)
+__device__ __forceinline__ uint64_t level_row(const Smem &m, const int *lvoff, int l, int y, int z, uint32_t &xr)
 {
 	constexpr int R = Geo<RB>::R;
-	if (l == 0) {
-		uint32_t xr;
-		uint64_t row = e0_row<RB>(m, y, z, xr);
-		return x == R ? xr : (uint32_t)((row >> x) & 1ull);
-	}
+	if (l == 0) return e0_row<RB>(m, y, z, xr);
+	xr = 0;
 	const int n = (R >> l) + 1;
-	return (uint32_t)((m.lv[lvoff[l] + z * n + y] >> x) & 1ull);
+	return m.lv[lvoff[l] + z * n + y];
 }
 
-/* Colour of the L0 mask cell (x, y, z) in [0, R]^3. */
+/* Colour of the L0 mask cell (x, y, z) in [0, R]^3: our own voxel, or the
+ * +neighbour's voxel for cells at coordinate R (read from its shell). */
 template <int RB>
-__device__ __forceinline__ uint32_t mask_colour(const uint32_t *__restrict__ s, const Smem &m, int x, int y, int z)
+__device__ __forceinline__ uint32_t mask_colour(const SetDesc &S, const uint32_t *__restrict__ s, const Smem &m,
+						int x, int y, int z)
 {
-	constexpr int R = Geo<RB>::R, RR = Geo<RB>::RR;
-	if (x == R) return m.col[(z << RB) | y];
-	if (y == R) return m.col[RR + ((z << RB) | x)];
-	if (z == R) return m.col[2 * RR + ((y << RB) | x)];
-	return colour_at<RB>(s, m, x, y, z);
+	using G = Geo<RB>;
+	constexpr int R = G::R, RR = G::RR;
+	int a = -1, idx = 0;
+	if (x == R) { a = 0; idx = (z << RB) | y; }
+	else if (y == R) { a = 1; idx = (z << RB) | x; }
+	else if (z == R) { a = 2; idx = (y << RB) | x; }
+	if (a < 0) return colour_at<RB>(s, m, x, y, z);
+	const int32_t nc = m.nbr[nbr_slot(a == 0, a == 1, a == 2)];
+	if (nc < 0) return 0u;
+	return S.shell_col[(size_t)nc * G::shell_cols + (size_t)a * RR + idx];
 }
 
 static __device__ __forceinline__ void store_splat(int16_t *dst, uint32_t x, uint32_t y, uint32_t z, uint32_t w)
@@ -444,6 +470,50 @@ static __device__ __forceinline__ void store_splat(int16_t *dst, uint32_t x, uin
 	v.x = (x & 0xFFFFu) | ((y & 0xFFFFu) << 16);
 	v.y = (z & 0xFFFFu) | ((w & 0xFFFFu) << 16);
 	*(uint2 *)dst = v;
+}
+
+/* Position of the k-th (0-based) set bit of v. */
+__device__ __forceinline__ int select_bit(uint64_t v, int k)
+{
+	int pos = 0;
+	uint32_t w = (uint32_t)v;
+	int c = __popc(w);
+	if (k >= c) {
+		k -= c;
+		w = (uint32_t)(v >> 32);
+		pos = 32;
+	}
+	c = __popc(w & 0xFFFFu);
+	if (k >= c) { k -= c; w >>= 16; pos += 16; }
+	c = __popc(w & 0xFFu);
+	if (k >= c) { k -= c; w >>= 8; pos += 8; }
+	c = __popc(w & 0xFu);
+	if (k >= c) { k -= c; w >>= 4; pos += 4; }
+	c = __popc(w & 0x3u);
+	if (k >= c) { k -= c; w >>= 2; pos += 2; }
+	c = (int)(w & 1u);
+	if (k >= c) pos += 1;
+	return pos;
+}
+
+/* For item j of a warp's group, the lane s (largest with excl[s] <= j) whose
+ * row holds it. All lanes must call it. */
+__device__ __forceinline__ int search_lane(uint32_t excl, uint32_t j)
+{
+	int s = 0;
+#pragma unroll
+	for (int step = 16; step; step >>= 1) {
+		const uint32_t o = __shfl_sync(kFull, excl, s + step);
+		if (o <= j) s += step;
+	}
+	return s;
+}
+
+__device__ __forceinline__ uint64_t shfl64(uint64_t v, int src)
+{
+	const uint32_t lo = __shfl_sync(kFull, (uint32_t)v, src);
+	const uint32_t hi = __shfl_sync(kFull, (uint32_t)(v >> 32), src);
+	return ((uint64_t)hi << 32) | lo;
 }
 
 /* Quad vertex offsets per visible face axis (lutv, src/chunkset/mesher.c:19-33)
@@ -456,21 +526,18 @@ __constant__ uint8_t c_quad_offset[3][4][3] = {
 __constant__ uint8_t c_quad_index[24] = {0, 3, 1, 2, 1, 3, 3, 2, 0, 1, 0, 2,
 					 1, 3, 0, 3, 1, 2, 0, 2, 3, 2, 0, 1};
 
+/* One face: AO from the 8 samples around the air voxel, shadow / diamond
+ * from the shadow map, 4 vertices and 6 indices (src/chunkset/mesher.c:
+ * 236-349). */
 template <int RB>
 __device__ void emit_face(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m, const uint32_t cv[3],
 			  int x, int y, int z, int i, uint32_t ordinal, int16_t *vbo, uint32_t *ibo)
 {
-	constexpr int R = Geo<RB>::R;
 	const int AC[3] = {x, y, z};
 	int NB[3] = {x, y, z};
 	NB[i] += 1;
 	const uint32_t a_solid = occ_at<RB>(m, x, y, z);
-	uint32_t colour;
-	if (a_solid) {
-		colour = colour_at<RB>(stream, m, x, y, z);
-	} else {
-		colour = mask_colour<RB>(stream, m, NB[0], NB[1], NB[2]);
-	}
+	const uint32_t colour = a_solid ? colour_at<RB>(stream, m, x, y, z) : mask_colour<RB>(S, stream, m, NB[0], NB[1], NB[2]);
 	const int normal = a_solid ? 0 : 1;
 	const int *AIR = a_solid ? NB : AC;
 	const int *BLK = a_solid ? AC : NB;
@@ -504,8 +571,7 @@ __device__ void emit_face(const SetDesc &S, const uint32_t *__restrict__ stream,
 	uint32_t diamond = 3;
 	if (i == 2) {
 		shadow = 0;
-		const uint32_t b_solid = a_solid ? 0u : 1u;
-		const uint32_t sz = ws[2] + (b_solid ? 0u : 1u);
+		const uint32_t sz = ws[2] + (a_solid ? 1u : 0u); /* +1 when B is air */
 		diamond = (uint32_t)(!shadow_sample(S, ws[0], ws[1], sz)) << 1;
 		diamond |= (uint32_t)(!shadow_sample(S, ws[0], ws[1] - 1u, sz));
 	}
@@ -530,6 +596,46 @@ __device__ void emit_face(const SetDesc &S, const uint32_t *__restrict__ stream,
 	id[2] = make_uint2(vb + qi[4], vb + qi[5]);
 }
 
+/* Face bits of row (y, z): bit x of f[i] = face between (x,y,z) and its
+ * +axis-i neighbour (exactly one of them solid). */
+template <int RB>
+__device__ __forceinline__ void face_bits(const Smem &m, int y, int z, uint64_t &fx, uint64_t &fy, uint64_t &fz)
+{
+	using G = Geo<RB>;
+	constexpr int R = G::R;
+	const uint64_t o = m.occ[hidx<RB>(y, z)];
+	fx = (o ^ ((o >> 1) | (xhi_bit<RB>(m, y, z) << (R - 1)))) & G::MASK;
+	fy = o ^ m.occ[hidx<RB>(y + 1, z)];
+	fz = o ^ m.occ[hidx<RB>(y, z + 1)];
+}
+
+/* (x, axis) of the k-th face of a row, faces ordered by x then axis. */
+template <int RB>
+__device__ __forceinline__ void select_face(uint64_t fx, uint64_t fy, uint64_t fz, uint32_t k, int &x, int &i)
+{
+	constexpr int R = Geo<RB>::R;
+	int pos = 0;
+#pragma unroll
+	for (int step = R / 2; step; step >>= 1) {
+		const int t = pos + step;
+		const uint64_t below = (1ull << t) - 1ull;
+		const uint32_t c = __popcll(fx & below) + __popcll(fy & below) + __popcll(fz & below);
+		if (c <= k) pos = t;
+	}
+	const uint64_t below = pos ? ((1ull << pos) - 1ull) : 0ull;
+	uint32_t r = k - (__popcll(fx & below) + __popcll(fy & below) + __popcll(fz & below));
+	const uint32_t b0 = (uint32_t)((fx >> pos) & 1ull), b1 = (uint32_t)((fy >> pos) & 1ull);
+	x = pos;
+	if (b0) {
+		if (r == 0) { i = 0; return; }
+		r--;
+	}
+	if (b1) {
+		if (r == 0) { i = 1; return; }
+	}
+	i = 2;
+}
+
 template <int RB>
 __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m, const uint32_t cv[3],
 			   ChunkOut *out, const Arena &avbo, const Arena &aibo)
@@ -537,22 +643,34 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
 	using G = Geo<RB>;
 	constexpr int R = G::R, RR = G::RR;
 	__shared__ unsigned long long s_base[2];
-	__shared__ uint32_t s_ok;
-	for (int r = threadIdx.x; r < RR; r += blockDim.x) {
-		const int y = r & (R - 1), z = r >> RB;
-		const uint64_t o = m.occ[hidx<RB>(y, z)];
-		const uint64_t fx = (o ^ ((o >> 1) | ((uint64_t)m.xhi[hidx<RB>(y, z)] << (R - 1)))) & G::MASK;
-		const uint64_t fy = o ^ m.occ[hidx<RB>(y + 1, z)];
-		const uint64_t fz = o ^ m.occ[hidx<RB>(y, z + 1)];
-		m.rowoff[r] = __popcll(fx) + __popcll(fy) + __popcll(fz);
+	__shared__ uint32_t s_ok, s_faces;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	const int seg = (RR + nw - 1) / nw;
+	const int lo = warp * seg, hi = min(RR, lo + seg);
+	/* pass 1: faces per warp range */
+	uint32_t cnt = 0;
+	for (int r = lo + lane; r < hi; r += 32) {
+		uint64_t fx, fy, fz;
+		face_bits<RB>(m, r & (R - 1), r >> RB, fx, fy, fz);
+		cnt += __popcll(fx) + __popcll(fy) + __popcll(fz);
+	}
+#pragma unroll
+	for (int d = 16; d; d >>= 1) cnt += __shfl_xor_sync(kFull, cnt, d);
+	if (lane == 0) m.wb[warp] = cnt;
+	__syncthreads();
+	if (warp == 0) {
+		const uint32_t v = lane < nw ? m.wb[lane] : 0u;
+		const uint32_t inc = warp_incl_add(v);
+		if (lane < nw) m.wb[lane] = inc - v;
+		if (lane == 31) s_faces = inc;
 	}
 	__syncthreads();
-	const uint32_t faces = block_scan_array(m.rowoff, RR, m.tmp);
+	const uint32_t faces = s_faces;
 	if (threadIdx.x == 0) {
 		const uint64_t uv = (uint64_t)faces * 2u;             /* 32 B per face */
 		const uint64_t ui = ((uint64_t)faces * 24u + 15u) / 16u;
-		unsigned long long bv = atomicAdd(avbo.cursor, (unsigned long long)uv);
-		unsigned long long bi = atomicAdd(aibo.cursor, (unsigned long long)ui);
+		unsigned long long bv = uv ? atomicAdd(avbo.cursor, (unsigned long long)uv) : 0ull;
+		unsigned long long bi = ui ? atomicAdd(aibo.cursor, (unsigned long long)ui) : 0ull;
 		uint32_t ok = (bv + uv <= avbo.cap_units) && (bi + ui <= aibo.cap_units);
 		s_base[0] = bv;
 		s_base[1] = bi;
@@ -570,31 +688,75 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
 	if (!s_ok || faces == 0) return;
 	int16_t *vbo = (int16_t *)avbo.base + s_base[0] * 8u;
 	uint32_t *ibo = (uint32_t *)aibo.base + s_base[1] * 4u;
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-	for (int r = warp; r < RR; r += nw) {
-		const int y = r & (R - 1), z = r >> RB;
-		const uint64_t o = m.occ[hidx<RB>(y, z)];
-		const uint64_t fx = (o ^ ((o >> 1) | ((uint64_t)m.xhi[hidx<RB>(y, z)] << (R - 1)))) & G::MASK;
-		const uint64_t fy = o ^ m.occ[hidx<RB>(y + 1, z)];
-		const uint64_t fz = o ^ m.occ[hidx<RB>(y, z + 1)];
-		uint32_t base = m.rowoff[r];
-		for (int h = 0; h < (R + 31) / 32; h++) {
-			const int x = 32 * h + lane;
-			uint32_t b0 = 0, b1 = 0, b2 = 0;
-			if (x < R) {
-				b0 = (uint32_t)((fx >> x) & 1ull);
-				b1 = (uint32_t)((fy >> x) & 1ull);
-				b2 = (uint32_t)((fz >> x) & 1ull);
+	/* pass 2: 32 rows per step, one face per lane */
+	uint32_t base = m.wb[warp];
+	for (int g = lo; g < hi; g += 32) {
+		const int r = g + lane;
+		uint64_t fx = 0, fy = 0, fz = 0;
+		if (r < hi) face_bits<RB>(m, r & (R - 1), r >> RB, fx, fy, fz);
+		const uint32_t c = __popcll(fx) + __popcll(fy) + __popcll(fz);
+		const uint32_t inc = warp_incl_add(c);
+		const uint32_t excl = inc - c;
+		const uint32_t T = __shfl_sync(kFull, inc, 31);
+		for (uint32_t k = 0; k < T; k += 32) {
+			const uint32_t j = k + lane;
+			const int s = search_lane(excl, j);
+			const uint32_t es = __shfl_sync(kFull, excl, s);
+			const uint64_t sx = shfl64(fx, s), sy = shfl64(fy, s), sz = shfl64(fz, s);
+			if (j < T) {
+				int x, i;
+				select_face<RB>(sx, sy, sz, j - es, x, i);
+				const int rr = g + s;
+				emit_face<RB>(S, stream, m, cv, x, rr & (R - 1), rr >> RB, i, base + j, vbo, ibo);
 			}
-			const uint32_t n = b0 + b1 + b2;
-			const uint32_t inc = warp_incl_add(n);
-			uint32_t ord = base + inc - n;
-			if (b0) emit_face<RB>(S, stream, m, cv, x, y, z, 0, ord++, vbo, ibo);
-			if (b1) emit_face<RB>(S, stream, m, cv, x, y, z, 1, ord++, vbo, ibo);
-			if (b2) emit_face<RB>(S, stream, m, cv, x, y, z, 2, ord++, vbo, ibo);
-			base += __shfl_sync(kFull, inc, 31);
 		}
+		base += T;
 	}
+}
+
+/* One level-l splat: walk down to the L0 cell whose colour the reference's
+ * last-writer-wins downsample keeps (the nonzero child with the largest
+ * (z, y, x) at every level, src/chunkset/mesher.c:474-489), then emit
+ * {x, y, z, colour | shadow << 6} (src/chunkset/mesher.c:521-531). */
+template <int RB>
+__device__ __forceinline__ void emit_splat(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m,
+					   const uint32_t cv[3], const int *lvoff, int l, int x, int y, int z, int16_t *dst)
+{
+	constexpr int R = Geo<RB>::R;
+	int cx = x, cy = y, cz = z;
+	for (int k2 = l; k2 >= 1; k2--) {
+		const int np = (R >> (k2 - 1)) + 1;
+		uint64_t rows[2][2];
+		uint32_t rx[2][2];
+		for (int dz = 0; dz < 2; dz++)
+			for (int dy = 0; dy < 2; dy++) {
+				const int Y = 2 * cy + dy, Z = 2 * cz + dz;
+				rows[dz][dy] = 0;
+				rx[dz][dy] = 0;
+				if (Y < np && Z < np) rows[dz][dy] = level_row<RB>(m, lvoff, k2 - 1, Y, Z, rx[dz][dy]);
+			}
+		int best = 0;
+		for (int d = 7; d >= 0; d--) {
+			const int dx = d & 1, dy = (d >> 1) & 1, dz = d >> 2;
+			const int X = 2 * cx + dx;
+			if (X >= np) continue;
+			const uint32_t bit = (k2 == 1 && X == R) ? rx[dz][dy] : (uint32_t)((rows[dz][dy] >> X) & 1ull);
+			if (bit) {
+				best = d;
+				break;
+			}
+		}
+		cx = 2 * cx + (best & 1);
+		cy = 2 * cy + ((best >> 1) & 1);
+		cz = 2 * cz + (best >> 2);
+	}
+	const uint32_t colour = mask_colour<RB>(S, stream, m, cx, cy, cz);
+	const uint32_t sh = l ? (1u << l) : 0u;
+	const uint32_t wx = (cv[0] << RB) + ((uint32_t)x << l);
+	const uint32_t wy = (cv[1] << RB) + ((uint32_t)y << l);
+	const uint32_t wz = (cv[2] << RB) + ((uint32_t)z << l);
+	const uint32_t shadow = (uint32_t)shadow_sample(S, wx + sh, wy + sh, wz + sh);
+	store_splat(dst, wx, wy, wz, colour | (shadow << 6));
 }
 
 template <int RB>
@@ -602,7 +764,7 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 			    int lod_max, ChunkOut *out, const Arena &asvl)
 {
 	using G = Geo<RB>;
-	constexpr int R = G::R, RR = G::RR, S1 = G::S;
+	constexpr int R = G::R, S1 = G::S;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 	__shared__ uint32_t s_cnt[kMaxLevels];
 	__shared__ unsigned long long s_base;
@@ -616,37 +778,6 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 		}
 		lvoff[0] = 0;
 	}
-	if (threadIdx.x < kMaxLevels) s_cnt[threadIdx.x] = 0;
-	/* L0 exposure rows (src/chunkset/mesher.c:421-446 restated per bit):
-	 * a solid voxel is in the mask when any +axis neighbour (the +chunk at
-	 * coordinate R) is air, or a -axis neighbour inside the chunk is air. */
-	for (int r = threadIdx.x; r < RR; r += blockDim.x) {
-		const int y = r & (R - 1), z = r >> RB;
-		const uint64_t o = m.occ[hidx<RB>(y, z)];
-		const uint64_t xp = (o >> 1) | ((uint64_t)m.xhi[hidx<RB>(y, z)] << (R - 1));
-		const uint64_t xm = ((o << 1) | 1ull) & G::MASK;
-		const uint64_t yp = m.occ[hidx<RB>(y + 1, z)];
-		const uint64_t ym = y ? m.occ[hidx<RB>(y - 1, z)] : G::MASK;
-		const uint64_t zp = m.occ[hidx<RB>(y, z + 1)];
-		const uint64_t zm = z ? m.occ[hidx<RB>(y, z - 1)] : G::MASK;
-		m.e0[r] = o & ~(xp & xm & yp & ym & zp & zm);
-	}
-	/* cells at coordinate R: the +neighbour's voxel is solid and ours air */
-	for (int z = warp; z < R; z += nw) {
-		uint64_t b = 0;
-		for (int h = 0; h < (R + 31) / 32; h++) {
-			const int y = 32 * h + lane;
-			bool bit = false;
-			if (y < R) bit = m.xhi[hidx<RB>(y, z)] && !((m.occ[hidx<RB>(y, z)] >> (R - 1)) & 1ull);
-			b |= (uint64_t)__ballot_sync(kFull, bit) << (32 * h);
-		}
-		if (lane == 0) m.e0p[z] = b & G::MASK;
-	}
-	for (int v = threadIdx.x; v < R; v += blockDim.x) {
-		m.e0p[R + v] = m.occ[hidx<RB>(R, v)] & ~m.occ[hidx<RB>(R - 1, v)];
-		m.e0p[2 * R + v] = m.occ[hidx<RB>(v, R)] & ~m.occ[hidx<RB>(v, R - 1)];
-	}
-	__syncthreads();
 	/* level rows: pairwise OR of the child rows, compacted along x */
 	for (int l = 1; l <= lod_max; l++) {
 		const int n = (R >> l) + 1, np = (R >> (l - 1)) + 1;
@@ -659,13 +790,9 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 				for (int dy = 0; dy < 2; dy++) {
 					const int yy = 2 * y + dy, zz = 2 * z + dz;
 					if (yy >= np || zz >= np) continue;
-					if (l == 1) {
-						uint32_t xr;
-						acc |= e0_row<RB>(m, yy, zz, xr);
-						accx |= xr;
-					} else {
-						acc |= m.lv[lvoff[l - 1] + zz * np + yy];
-					}
+					uint32_t xr;
+					acc |= level_row<RB>(m, lvoff, l - 1, yy, zz, xr);
+					accx |= xr;
 				}
 			uint64_t row = compress_pairs(acc);
 			if (l == 1) row |= (uint64_t)accx << (R / 2);
@@ -673,131 +800,97 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 		}
 		__syncthreads();
 	}
-	/* counts per level */
-	{
-		uint32_t c0 = 0;
-		for (int r = threadIdx.x; r < RR; r += blockDim.x) c0 += __popcll(m.e0[r]);
-		for (int r = threadIdx.x; r < 3 * R; r += blockDim.x) c0 += __popcll(m.e0p[r]);
-		for (int d = 16; d; d >>= 1) c0 += __shfl_xor_sync(kFull, c0, d);
-		if (lane == 0 && c0) atomicAdd(&s_cnt[0], c0);
-		for (int l = 1; l <= lod_max; l++) {
-			const int n = (R >> l) + 1;
-			uint32_t c = 0;
-			for (int i = threadIdx.x; i < n * n; i += blockDim.x) c += __popcll(m.lv[lvoff[l] + i]);
-			for (int d = 16; d; d >>= 1) c += __shfl_xor_sync(kFull, c, d);
-			if (lane == 0 && c) atomicAdd(&s_cnt[l], c);
+	/* pass 1: splats per level per warp range */
+	for (int l = 0; l <= lod_max; l++) {
+		const int n = l ? (R >> l) + 1 : S1;
+		const int seg = (n * n + nw - 1) / nw;
+		const int lo = warp * seg, hi = min(n * n, lo + seg);
+		uint32_t c = 0;
+		for (int i = lo + lane; i < hi; i += 32) {
+			uint32_t xr;
+			c += __popcll(level_row<RB>(m, lvoff, l, i % n, i / n, xr)) + xr;
 		}
+#pragma unroll
+		for (int d = 16; d; d >>= 1) c += __shfl_xor_sync(kFull, c, d);
+		if (lane == 0) m.wb[l * 16 + warp] = c;
 	}
 	__syncthreads();
-	if (threadIdx.x == 0) {
-		uint32_t total = 0;
-		for (int l = 0; l <= lod_max; l++) total += s_cnt[l];
-		const uint64_t units = ((uint64_t)total + 1u) / 2u; /* 8 B per splat */
-		unsigned long long b = units ? atomicAdd(asvl.cursor, (unsigned long long)units) : 0ull;
-		const uint32_t ok = (b + units <= asvl.cap_units);
-		s_base = b;
-		s_ok = ok;
-		out->svl_off = b * 8u;
-		out->svl_total = total * 4u;
-		for (int l = 0; l < kMaxLevels; l++) out->svl_items[l] = l <= lod_max ? s_cnt[l] * 4u : 0u;
-		out->vbo_off = out->ibo_off = 0;
-		out->vbo_items = out->ibo_items = 0;
-		out->status = ok ? 0u : kStatusOverflow;
+	if (warp == 0) {
+		uint32_t level_base = 0;
+		for (int l = 0; l <= lod_max; l++) {
+			const uint32_t v = lane < nw ? m.wb[l * 16 + lane] : 0u;
+			const uint32_t inc = warp_incl_add(v);
+			if (lane < nw) m.wb[l * 16 + lane] = level_base + inc - v;
+			const uint32_t tot = __shfl_sync(kFull, inc, 31);
+			if (lane == 0) s_cnt[l] = tot;
+			level_base += tot;
+		}
+		if (lane == 0) {
+			const uint32_t total = level_base;
+			const uint64_t units = ((uint64_t)total + 1u) / 2u; /* 8 B per splat */
+			unsigned long long b = units ? atomicAdd(asvl.cursor, (unsigned long long)units) : 0ull;
+			const uint32_t ok = (b + units <= asvl.cap_units);
+			s_base = b;
+			s_ok = ok;
+			out->svl_off = b * 8u;
+			out->svl_total = total * 4u;
+			for (int l = 0; l < kMaxLevels; l++) out->svl_items[l] = l <= lod_max ? s_cnt[l] * 4u : 0u;
+			out->vbo_off = out->ibo_off = 0;
+			out->vbo_items = out->ibo_items = 0;
+			out->status = ok ? 0u : kStatusOverflow;
+		}
 	}
 	__syncthreads();
 	if (!s_ok) return;
 	int16_t *dst = (int16_t *)asvl.base + s_base * 8u;
-	uint32_t level_base = 0;
+	/* pass 2: 32 rows per step, one splat per lane */
 	for (int l = 0; l <= lod_max; l++) {
 		const int n = l ? (R >> l) + 1 : S1;
-		/* row counts and their scan */
-		for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
-			const int y = i % n, z = i / n;
-			uint32_t c;
-			if (l == 0) {
-				uint32_t xr;
-				c = __popcll(e0_row<RB>(m, y, z, xr)) + xr;
-			} else {
-				c = __popcll(m.lv[lvoff[l] + i]);
-			}
-			m.rowoff[i] = c;
-		}
-		__syncthreads();
-		block_scan_array(m.rowoff, n * n, m.tmp);
-		const uint32_t sh = l ? (1u << l) : 0u;
-		for (int i = warp; i < n * n; i += nw) {
-			const int y = i % n, z = i / n;
-			uint64_t row;
+		const int seg = (n * n + nw - 1) / nw;
+		const int lo = warp * seg, hi = min(n * n, lo + seg);
+		uint32_t base = m.wb[l * 16 + warp];
+		for (int g = lo; g < hi; g += 32) {
+			const int r = g + lane;
+			uint64_t row = 0;
 			uint32_t xr = 0;
-			if (l == 0)
-				row = e0_row<RB>(m, y, z, xr);
-			else
-				row = m.lv[lvoff[l] + i];
-			if (!row && !xr) continue;
-			uint32_t base = level_base + m.rowoff[i];
-			const int nbits = l ? n : R; /* x = R of level 0 handled after */
-			for (int h = 0; h < (nbits + 31) / 32; h++) {
-				const int x = 32 * h + lane;
-				const bool bit = x < nbits && ((row >> x) & 1ull);
-				const uint32_t bal = __ballot_sync(kFull, bit);
-				if (bit) {
-					const uint32_t k = base + __popc(bal & ((1u << lane) - 1u));
-					int cx = x, cy = y, cz = z;
-					for (int k2 = l; k2 >= 1; k2--) {
-						const int np = (R >> (k2 - 1)) + 1;
-						int best = 0;
-						for (int d = 7; d >= 0; d--) {
-							const int X = 2 * cx + (d & 1), Y = 2 * cy + ((d >> 1) & 1),
-								  Z = 2 * cz + (d >> 2);
-							if (X < np && Y < np && Z < np && level_bit<RB>(m, lvoff, k2 - 1, X, Y, Z)) {
-								best = d;
-								break;
-							}
-						}
-						cx = 2 * cx + (best & 1);
-						cy = 2 * cy + ((best >> 1) & 1);
-						cz = 2 * cz + (best >> 2);
-					}
-					const uint32_t colour = mask_colour<RB>(stream, m, cx, cy, cz);
-					const uint32_t wx = (cv[0] << RB) + ((uint32_t)x << l);
-					const uint32_t wy = (cv[1] << RB) + ((uint32_t)y << l);
-					const uint32_t wz = (cv[2] << RB) + ((uint32_t)z << l);
-					const uint32_t sh_ = (uint32_t)shadow_sample(S, wx + sh, wy + sh, wz + sh);
-					store_splat(dst + (size_t)k * 4, wx, wy, wz, colour | (sh_ << 6));
+			if (r < hi) row = level_row<RB>(m, lvoff, l, r % n, r / n, xr);
+			const uint32_t c = __popcll(row) + xr;
+			const uint32_t inc = warp_incl_add(c);
+			const uint32_t excl = inc - c;
+			const uint32_t T = __shfl_sync(kFull, inc, 31);
+			for (uint32_t k = 0; k < T; k += 32) {
+				const uint32_t j = k + lane;
+				const int s = search_lane(excl, j);
+				const uint32_t es = __shfl_sync(kFull, excl, s);
+				const uint64_t srow = shfl64(row, s);
+				if (j < T) {
+					const int kk = (int)(j - es);
+					const int x = kk < __popcll(srow) ? select_bit(srow, kk) : R;
+					const int rr = g + s;
+					emit_splat<RB>(S, stream, m, cv, lvoff, l, x, rr % n, rr / n,
+						       dst + (size_t)(base + j) * 4);
 				}
-				base += __popc(bal);
 			}
-			if (l == 0 && xr && lane == 0) {
-				const uint32_t colour = mask_colour<RB>(stream, m, R, y, z);
-				const uint32_t wx = (cv[0] << RB) + (uint32_t)R;
-				const uint32_t wy = (cv[1] << RB) + (uint32_t)y;
-				const uint32_t wz = (cv[2] << RB) + (uint32_t)z;
-				const uint32_t sh_ = (uint32_t)shadow_sample(S, wx, wy, wz);
-				store_splat(dst + (size_t)base * 4, wx, wy, wz, colour | (sh_ << 6));
-			}
+			base += T;
 		}
-		level_base += s_cnt[l];
-		__syncthreads();
 	}
 }
 
 template <int RB>
-__global__ void __launch_bounds__(512) k_geometry(const SetDesc *__restrict__ sets, const WorkItem *__restrict__ items,
-						  uint32_t nitems, unsigned int *queue, ChunkOut *outs, Arena asvl,
-						  Arena avbo, Arena aibo, int lod_max)
+__global__ void __launch_bounds__(512, 2) k_geometry(const SetDesc *__restrict__ sets, const WorkItem *__restrict__ items,
+						     uint32_t nitems, unsigned int *queue, ChunkOut *outs, Arena asvl,
+						     Arena avbo, Arena aibo, int lod_max)
 {
 	using G = Geo<RB>;
 	constexpr int R = G::R;
 	extern __shared__ __align__(16) uint8_t smem[];
 	const Smem m = carve<RB>(smem);
 	__shared__ uint32_t s_item;
-	(void)sizeof(G);
 	uint32_t next = blockIdx.x;
 	for (;;) {
 		if (threadIdx.x == 0) s_item = queue ? atomicAdd(queue, 1u) : next;
 		__syncthreads();
 		const uint32_t it = s_item;
-		__syncthreads();
 		if (it >= nitems) break;
 		next = nitems;
 		const WorkItem wi = items[it];
@@ -807,12 +900,10 @@ __global__ void __launch_bounds__(512) k_geometry(const SetDesc *__restrict__ se
 		chunk_coords(S, wi.chunk, cv);
 		const uint32_t N = (uint32_t)R * R * R;
 		const bool mesh = (wi.flags & kItemMesh) != 0;
+		load_neighbours(S, cv, m, N);
 		/* an all-air chunk whose +neighbours are all air has no geometry */
-		bool empty = chunk_is_null(S, wi.chunk, N);
-		for (int a = 0; a < 3 && empty; a++) {
-			const int64_t nc = neighbour(S, cv, a == 0, a == 1, a == 2);
-			if (nc >= 0 && !chunk_is_null(S, (uint32_t)nc, N)) empty = false;
-		}
+		const bool empty = m.nbr[nbr_slot(0, 0, 0)] < 0 && m.nbr[nbr_slot(1, 0, 0)] < 0 &&
+				   m.nbr[nbr_slot(0, 1, 0)] < 0 && m.nbr[nbr_slot(0, 0, 1)] < 0;
 		if (empty) {
 			if (threadIdx.x == 0) {
 				out->svl_off = out->vbo_off = out->ibo_off = 0;
@@ -820,11 +911,12 @@ __global__ void __launch_bounds__(512) k_geometry(const SetDesc *__restrict__ se
 				out->svl_total = out->vbo_items = out->ibo_items = 0;
 				out->status = 0;
 			}
+			__syncthreads();
 			continue;
 		}
 		const uint32_t *stream = S.pool + S.off[wi.chunk];
 		decode_chunk<RB>(stream, S.len[wi.chunk] - 1u, m);
-		load_halo<RB>(S, cv, m, mesh);
+		load_halo<RB>(S, m);
 		if (mesh)
 			mesh_chunk<RB>(S, stream, m, cv, out, avbo, aibo);
 		else
