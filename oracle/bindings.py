@@ -110,6 +110,15 @@ class _Base:
         return vbo[:int(nv[0])].copy(), ibo[:int(ni[0])].copy()
 
 
+class _VpoWorldHead(ctypes.Structure):
+    """Leading fields of struct vpo_world (oracle/vpo.h)."""
+    _fields_ = [("root_bitw", ctypes.c_int), ("R", ctypes.c_int), ("max_bitw", ctypes.c_int * 3),
+                ("max", ctypes.c_int * 3), ("nchunks", ctypes.c_uint32),
+                ("rle", ctypes.c_void_p), ("rle_len", ctypes.c_void_p), ("vox", ctypes.c_void_p),
+                ("shadow", ctypes.POINTER(ctypes.c_uint16)), ("shadow_len", ctypes.c_uint64),
+                ("shadow_w", ctypes.c_uint32), ("shadow_z", ctypes.c_uint32)]
+
+
 class OracleWorld(_Base):
     def __init__(self, world):
         lib = vpo_lib()
@@ -158,9 +167,10 @@ class OracleWorld(_Base):
         self.lib.vpo_edit_sphere(self.h, _vp(ws), r, v, _vp(dirty))
         return dirty
 
-    def shadow(self, n):
-        # shadow pointer lives in the struct; read via a helper world copy
-        raise NotImplementedError
+    def shadow_map(self):
+        """The (padded) shadow map, e.g. after edits."""
+        w = ctypes.cast(self.h, ctypes.POINTER(_VpoWorldHead)).contents
+        return np.ctypeslib.as_array(w.shadow, shape=(w.shadow_len,)).copy()
 
 
 class RefWorld(_Base):

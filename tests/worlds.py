@@ -70,3 +70,20 @@ def compare_world(gpu_world, oracle, make_mesh, lod_max, chunks=None):
                 bad.append("chunk %d svl differs at %d: %s vs %s" % (c, k, g[k - k % 4:k - k % 4 + 4],
                                                                      og[k - k % 4:k - k % 4 + 4]))
     return bad
+
+
+def load_fixture(path):
+    """(World, dict of arrays) from a golden .npz written by make_golden.py."""
+    d = dict(np.load(path))
+    w = wg.World(int(d["root_bitw"]), tuple(int(b) for b in d["max_bitw"]), d["pool"], d["off"], d["len"],
+                 d["shadow"], int(d["shadow_w"]), int(d["shadow_z"]), int(d["pad_rows"]))
+    return w, d
+
+
+def split(flat, counts):
+    """Split a concatenation back into per-chunk pieces."""
+    out, o = [], 0
+    for c in counts:
+        out.append(flat[o:o + int(c)])
+        o += int(c)
+    return out

@@ -75,6 +75,7 @@ struct vp_world {
 	SetDesc *d_set = nullptr;
 	WorkItem *d_items = nullptr;
 	std::vector<uint8_t> modes;
+	std::vector<uint32_t> hlen;              /* host copy of stream lengths */
 	bool items_dirty = true;
 	ChunkOut *d_outs = nullptr;
 	unsigned int *d_queue = nullptr;
@@ -249,7 +250,7 @@ VP_API int vp_world_upload(vp_world *w, const uint32_t *pool, uint64_t pool_word
 		noff[c] = total;
 		total += (len[c] + 3u) & ~3u;
 	}
-	total += 4; /* vector loads may read up to 3 words past a terminator */
+	total += 8; /* vector loads may read up to 7 words past a terminator */
 	std::vector<uint32_t> packed(total, 0u);
 	for (uint32_t c = 0; c < w->nchunks; c++)
 		memcpy(&packed[noff[c]], pool + off[c], (size_t)len[c] * sizeof(uint32_t));
@@ -268,6 +269,8 @@ VP_API int vp_world_upload(vp_world *w, const uint32_t *pool, uint64_t pool_word
 	if (shadow_len)
 		CK(cudaMemcpyAsync(w->d_shadow, shadow, shadow_len * sizeof(uint16_t), cudaMemcpyHostToDevice, st));
 	w->pool_words = total;
+	w->hlen.assign(len, len + w->nchunks);
+	w->items_dirty = true;
 	w->shadow_len = shadow_len;
 	w->shadow_w = shadow_w;
 	w->uploaded = true;
@@ -285,12 +288,23 @@ VP_API int vp_world_set_modes(vp_world *w, const uint8_t *make_mesh)
 static int ensure_items(vp_world *w)
 {
 	if (!w->items_dirty) return VP_OK;
-	std::vector<WorkItem> it(w->nchunks);
+	/* longest first: a chunk's cost grows with its run count, and a meshed
+	 * chunk costs about three times a splatted one */
+	std::vector<uint32_t> order(w->nchunks);
+	std::vector<uint64_t> cost(w->nchunks);
 	for (uint32_t c = 0; c < w->nchunks; c++) {
-		it[c].set = 0;
-		it[c].chunk = c;
-		it[c].flags = w->modes[c] ? kItemMesh : 0u;
-		it[c].pad = 0;
+		order[c] = c;
+		const uint64_t len = c < w->hlen.size() ? w->hlen[c] : 2u;
+		cost[c] = (len + 64u) * (w->modes[c] ? 3u : 1u);
+	}
+	std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
+	std::vector<WorkItem> it(w->nchunks);
+	for (uint32_t k = 0; k < w->nchunks; k++) {
+		const uint32_t c = order[k];
+		it[k].set = 0;
+		it[k].chunk = c;
+		it[k].flags = w->modes[c] ? kItemMesh : 0u;
+		it[k].slot = c;
 	}
 	CK(cudaMemcpyAsync(w->d_items, it.data(), it.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
 			   w->ctx->stream));

@@ -44,7 +44,7 @@ struct WorkItem {
 	uint32_t set;
 	uint32_t chunk;
 	uint32_t flags;
-	uint32_t pad;
+	uint32_t slot;   /* index of the ChunkOut record this item fills */
 };
 
 /* Per work item result record. Offsets are in elements of the arena type. */
@@ -193,7 +193,8 @@ __device__ __forceinline__ int shadow_sample(const SetDesc &s, uint32_t x, uint3
 	uint32_t lim = y + 1u;
 	if (lim == 0u) return 1; /* nothing is < 0: shadowed whatever is read */
 	uint32_t idx = (x + y) + s.shadow_w * z;
-	return !(shadow_at(s, idx) < lim && shadow_at(s, idx + 1u) < lim);
+	const uint32_t a = shadow_at(s, idx), b = shadow_at(s, idx + 1u); /* both loads in flight */
+	return !((a < lim) & (b < lim));
 }
 
 /* shadow_sample_normal (src/chunkset/shadow.h:65-75) */
@@ -202,7 +203,8 @@ __device__ __forceinline__ int shadow_sample_normal(const SetDesc &s, uint32_t x
 	uint32_t lim = y + 1u;
 	if (lim == 0u) return 1;
 	uint32_t idx = (x + y) + s.shadow_w * z;
-	return !(shadow_at(s, idx) < lim && shadow_at(s, idx - 1u) < lim);
+	const uint32_t a = shadow_at(s, idx), b = shadow_at(s, idx - 1u);
+	return !((a < lim) & (b < lim));
 }
 
 } // namespace vp

@@ -54,8 +54,17 @@ struct Geo {
 	static constexpr size_t o_xrow = a16(o_lv + sizeof(uint64_t) * lv_words());
 	static constexpr size_t o_xedge = a16(o_xrow + sizeof(uint64_t) * 2 * H);
 	static constexpr size_t o_tmp = a16(o_xedge + 4 * H);
-	static constexpr size_t o_wb = a16(o_tmp + sizeof(uint32_t) * 64);
-	static constexpr size_t o_nbr = a16(o_wb + sizeof(uint32_t) * kMaxLevels * 16);
+	static constexpr int groups_of(int rows) { return (rows + 31) / 32; }
+	static constexpr int max_groups()
+	{
+		int t = 0;
+		for (int l = 0; l < kMaxLevels; l++) t += groups_of(n_at(l) * n_at(l));
+		return t > groups_of(RR) ? t : groups_of(RR);
+	}
+	static constexpr size_t o_grp = a16(o_tmp + sizeof(uint32_t) * 64);
+	static constexpr size_t o_e0p = a16(o_grp + sizeof(uint32_t) * (max_groups() + 1));
+	static constexpr size_t o_sv = a16(o_e0p + sizeof(uint64_t) * 3 * R);
+	static constexpr size_t o_nbr = a16(o_sv + sizeof(uint64_t) * 2 * R);
 	static constexpr size_t bytes = a16(o_nbr + sizeof(int32_t) * 28);
 	static constexpr size_t shell_words = 6 * R;   /* u64 per chunk */
 	static constexpr size_t shell_cols = 3 * RR;   /* bytes per chunk */
@@ -64,7 +73,9 @@ struct Geo {
 struct Smem {
 	uint64_t *occ, *rs, *lv;
 	uint32_t *rank, *tmp;
-	uint32_t *wb;    /* [level][warp] emission bases */
+	uint32_t *grp;   /* emission base of every 32-row group */
+	uint64_t *e0p;   /* splat mode: L0 mask rows of the x = R, y = R, z = R planes */
+	uint64_t *sv;    /* splat mode: two saved occupancy planes */
 	uint64_t *xrow;  /* [side][z+1]: x = -1 (side 0) / x = R (side 1), bits over y */
 	uint8_t *xedge;  /* [side*2 + (y == R)][z+1]: the y = -1 / y = R corners */
 	int32_t *nbr;    /* 27 neighbour chunk indices, -1 = air (outside or null) */
@@ -82,7 +93,9 @@ __device__ __forceinline__ Smem carve(uint8_t *base)
 	s.xrow = (uint64_t *)(base + G::o_xrow);
 	s.xedge = base + G::o_xedge;
 	s.tmp = (uint32_t *)(base + G::o_tmp);
-	s.wb = (uint32_t *)(base + G::o_wb);
+	s.grp = (uint32_t *)(base + G::o_grp);
+	s.e0p = (uint64_t *)(base + G::o_e0p);
+	s.sv = (uint64_t *)(base + G::o_sv);
 	s.nbr = (int32_t *)(base + G::o_nbr);
 	return s;
 }
@@ -131,58 +144,60 @@ __device__ void decode_chunk(const uint32_t *__restrict__ s, uint32_t nruns, con
 		m.rs[r] = 0;
 	}
 	__syncthreads();
+	(void)lane;
 	uint32_t *rs32 = (uint32_t *)m.rs;
 	uint32_t *occ32 = (uint32_t *)m.occ;
+	/* each thread owns 8 consecutive runs per tile; bits falling in the same
+	 * 32-bit word are combined in registers before one shared atomic */
+	constexpr int K = 8;
 	uint32_t tile_start = 0;
-	for (uint32_t base = 0; base < nruns; base += 4u * blockDim.x) {
-		const uint32_t k0 = base + 4u * threadIdx.x;
-		uint32_t w[4] = {0, 0, 0, 0};
-		if (k0 < nruns) {
-			uint4 q = __ldg((const uint4 *)(s + k0));
-			w[0] = q.x; w[1] = q.y; w[2] = q.z; w[3] = q.w;
+	for (uint32_t base = 0; base < nruns; base += (uint32_t)K * blockDim.x) {
+		const uint32_t k0 = base + (uint32_t)K * threadIdx.x;
+		uint32_t w[K];
 #pragma unroll
-			for (int j = 0; j < 4; j++)
+		for (int j = 0; j < K; j++) w[j] = 0;
+		if (k0 < nruns) {
+			const uint4 q0 = __ldg((const uint4 *)(s + k0));
+			const uint4 q1 = __ldg((const uint4 *)(s + k0 + 4));
+			w[0] = q0.x; w[1] = q0.y; w[2] = q0.z; w[3] = q0.w;
+			w[4] = q1.x; w[5] = q1.y; w[6] = q1.z; w[7] = q1.w;
+#pragma unroll
+			for (int j = 0; j < K; j++)
 				if (k0 + j >= nruns) w[j] = 0;
 		}
-		uint32_t c[4], sum = 0;
+		uint32_t sum = 0;
 #pragma unroll
-		for (int j = 0; j < 4; j++) {
-			c[j] = w[j] & 0xFFFFFFu;
-			sum += c[j];
-		}
+		for (int j = 0; j < K; j++) sum += w[j] & 0xFFFFFFu;
 		uint32_t tot;
 		uint32_t pos = tile_start + block_excl_add(sum, m.tmp, &tot);
-		uint32_t prev = (k0 > 0 && k0 < nruns) ? __ldg(s + k0 - 1) : 0u;
+		if (k0 < nruns) {
+			bool prev_solid = k0 > 0 ? ((__ldg(s + k0 - 1) >> 24) != 0) : false;
+			uint32_t cur = 0xFFFFFFFFu, acc_r = 0, acc_t = 0;
 #pragma unroll
-		for (int j = 0; j < 4; j++) {
-			const bool valid = k0 + j < nruns;
-			const uint32_t p = pos;
-			pos += c[j];
-			const uint32_t pc = j ? w[j - 1] : prev;
-			const bool tog = valid && (((w[j] >> 24) != 0) != ((pc >> 24) != 0));
-			uint32_t key = valid ? (p >> KB) : 0xFFFFFFFFu;
-			uint32_t vr = valid ? (1u << (p & ((1u << KB) - 1u))) : 0u;
-			uint32_t vt = tog ? vr : 0u;
-#pragma unroll
-			for (int d = 1; d < 32; d <<= 1) {
-				uint32_t k2 = __shfl_up_sync(kFull, key, d);
-				uint32_t a = __shfl_up_sync(kFull, vr, d);
-				uint32_t b = __shfl_up_sync(kFull, vt, d);
-				if (lane >= d && k2 == key) {
-					vr |= a;
-					vt |= b;
+			for (int j = 0; j < K; j++) {
+				if (k0 + j >= nruns) break;
+				const uint32_t p = pos;
+				pos += w[j] & 0xFFFFFFu;
+				const bool solid = (w[j] >> 24) != 0;
+				const uint32_t key = p >> KB;
+				if (key != cur) {
+					if (cur != 0xFFFFFFFFu) {
+						const uint32_t row = (cur << KB) >> RB, half = ((cur << KB) & (R - 1)) >> 5;
+						atomicOr(rs32 + 2 * row + half, acc_r);
+						if (acc_t) atomicOr(occ32 + 2 * hidx<RB>(row & (R - 1), row >> RB) + half, acc_t);
+					}
+					cur = key;
+					acc_r = acc_t = 0;
 				}
+				const uint32_t bit = 1u << (p & ((1u << KB) - 1u));
+				acc_r |= bit;
+				if (solid != prev_solid) acc_t |= bit;
+				prev_solid = solid;
 			}
-			uint32_t nk = __shfl_down_sync(kFull, key, 1);
-			const bool last = (lane == 31) || nk != key;
-			if (valid && last) {
-				const uint32_t row = p >> RB;
-				const uint32_t half = (p & (R - 1)) >> 5;
-				atomicOr(rs32 + 2 * row + half, vr);
-				if (vt) {
-					const int y = row & (R - 1), z = row >> RB;
-					atomicOr(occ32 + 2 * hidx<RB>(y, z) + half, vt);
-				}
+			if (cur != 0xFFFFFFFFu) {
+				const uint32_t row = (cur << KB) >> RB, half = ((cur << KB) & (R - 1)) >> 5;
+				atomicOr(rs32 + 2 * row + half, acc_r);
+				if (acc_t) atomicOr(occ32 + 2 * hidx<RB>(row & (R - 1), row >> RB) + half, acc_t);
 			}
 		}
 		tile_start += tot;
@@ -407,32 +422,74 @@ __device__ __forceinline__ uint32_t occ_at(const Smem &m, int x, int y, int z)
 	return (uint32_t)((m.occ[hidx<RB>(y, z)] >> x) & 1ull);
 }
 
-/* L0 mask row (y, z) in [0, R]^2 (src/chunkset/mesher.c:421-446 restated
- * per bit): a solid voxel is in the mask when any +axis neighbour (the
- * +chunk's voxel at coordinate R) is air, or a -axis neighbour inside the
- * chunk is air; a cell at coordinate R is in the mask when the +chunk's
- * voxel is solid and ours air. Bits x in [0, R); *xr = the x = R cell. */
+/* L0 mask row (y, z) in [0, R]^2 once splat_prepare has run: bits x in
+ * [0, R); *xr = the x = R cell. */
 template <int RB>
 __device__ __forceinline__ uint64_t e0_row(const Smem &m, int y, int z, uint32_t &xr)
 {
-	using G = Geo<RB>;
-	constexpr int R = G::R;
+	constexpr int R = Geo<RB>::R;
 	xr = 0;
 	if (y < R && z < R) {
-		const uint64_t o = m.occ[hidx<RB>(y, z)];
-		const uint64_t xh = xhi_bit<RB>(m, y, z);
-		xr = (uint32_t)(xh & ~(o >> (R - 1)) & 1ull);
-		const uint64_t xp = (o >> 1) | (xh << (R - 1));
-		const uint64_t xm = ((o << 1) | 1ull) & G::MASK;
-		const uint64_t yp = m.occ[hidx<RB>(y + 1, z)];
-		const uint64_t ym = y ? m.occ[hidx<RB>(y - 1, z)] : G::MASK;
-		const uint64_t zp = m.occ[hidx<RB>(y, z + 1)];
-		const uint64_t zm = z ? m.occ[hidx<RB>(y, z - 1)] : G::MASK;
-		return o & ~(xp & xm & yp & ym & zp & zm);
+		xr = (uint32_t)((m.e0p[z] >> y) & 1ull);
+		return m.occ[hidx<RB>(y, z)];
 	}
-	if (y == R && z < R) return m.occ[hidx<RB>(R, z)] & ~m.occ[hidx<RB>(R - 1, z)];
-	if (z == R && y < R) return m.occ[hidx<RB>(y, R)] & ~m.occ[hidx<RB>(y, R - 1)];
+	if (y == R && z < R) return m.e0p[R + z];
+	if (z == R && y < R) return m.e0p[2 * R + y];
 	return 0ull;
+}
+
+/* Replace the occupancy rows by the L0 mask rows (src/chunkset/mesher.c:
+ * 421-446 restated per bit): a solid voxel is in the mask when any +axis
+ * neighbour (the +chunk's voxel at coordinate R) is air, or a -axis
+ * neighbour inside the chunk is air; a cell at coordinate R is in the mask
+ * when the +chunk's voxel there is solid and ours air. Rows are rewritten in
+ * z-slabs; the last original plane of each slab is kept for the next. */
+template <int RB>
+__device__ void splat_prepare(const Smem &m)
+{
+	using G = Geo<RB>;
+	constexpr int R = G::R;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	for (int z = warp; z < R; z += nw) {
+		uint64_t b = 0;
+		for (int h = 0; h < (R + 31) / 32; h++) {
+			const int y = 32 * h + lane;
+			bool bit = false;
+			if (y < R) bit = xhi_bit<RB>(m, y, z) && !((m.occ[hidx<RB>(y, z)] >> (R - 1)) & 1ull);
+			b |= (uint64_t)__ballot_sync(kFull, bit) << (32 * h);
+		}
+		if (lane == 0) m.e0p[z] = b & G::MASK;
+	}
+	for (int v = threadIdx.x; v < R; v += blockDim.x) {
+		m.e0p[R + v] = m.occ[hidx<RB>(R, v)] & ~m.occ[hidx<RB>(R - 1, v)];
+		m.e0p[2 * R + v] = m.occ[hidx<RB>(v, R)] & ~m.occ[hidx<RB>(v, R - 1)];
+	}
+	__syncthreads();
+	const int P = min((int)blockDim.x / R, R); /* planes per slab */
+	int cur = 0;
+	for (int z0 = 0; z0 < R; z0 += P) {
+		const int t = threadIdx.x;
+		const bool act = t < P * R && z0 + t / R < R;
+		const int y = t & (R - 1), z = z0 + t / R;
+		uint64_t e = 0, o = 0;
+		if (act) {
+			o = m.occ[hidx<RB>(y, z)];
+			const uint64_t xp = (o >> 1) | (xhi_bit<RB>(m, y, z) << (R - 1));
+			const uint64_t xm = ((o << 1) | 1ull) & G::MASK;
+			const uint64_t yp = m.occ[hidx<RB>(y + 1, z)];
+			const uint64_t ym = y ? m.occ[hidx<RB>(y - 1, z)] : G::MASK;
+			const uint64_t zp = m.occ[hidx<RB>(y, z + 1)];
+			const uint64_t zm = z == 0 ? G::MASK : (z == z0 ? m.sv[cur * R + y] : m.occ[hidx<RB>(y, z - 1)]);
+			e = o & ~(xp & xm & yp & ym & zp & zm);
+		}
+		__syncthreads();
+		if (act) {
+			if (z == z0 + P - 1) m.sv[(cur ^ 1) * R + y] = o;
+			m.occ[hidx<RB>(y, z)] = e;
+		}
+		__syncthreads();
+		cur ^= 1;
+	}
 }
 
 /* Level-l mask row (y, z); level 0 includes the x = R cell in *xr. */
@@ -636,36 +693,52 @@ __device__ __forceinline__ void select_face(uint64_t fx, uint64_t fy, uint64_t f
 	i = 2;
 }
 
+/* Exclusive scan, in place, of n <= 32*8 group counts by warp 0; returns
+ * the total to all threads. */
+__device__ __forceinline__ uint32_t scan_groups(uint32_t *g, int n, uint32_t *tmp)
+{
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	if (warp == 0) {
+		uint32_t carry = 0;
+		for (int b = 0; b < n; b += 32) {
+			const int i = b + lane;
+			const uint32_t v = i < n ? g[i] : 0u;
+			const uint32_t inc = warp_incl_add(v);
+			if (i < n) g[i] = carry + inc - v;
+			carry += __shfl_sync(kFull, inc, 31);
+		}
+		if (lane == 0) tmp[0] = carry;
+	}
+	__syncthreads();
+	const uint32_t t = tmp[0];
+	__syncthreads();
+	return t;
+}
+
 template <int RB>
 __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m, const uint32_t cv[3],
 			   ChunkOut *out, const Arena &avbo, const Arena &aibo)
 {
 	using G = Geo<RB>;
-	constexpr int R = G::R, RR = G::RR;
+	constexpr int R = G::R, RR = G::RR, NG = (RR + 31) / 32;
 	__shared__ unsigned long long s_base[2];
-	__shared__ uint32_t s_ok, s_faces;
+	__shared__ uint32_t s_ok, s_next;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-	const int seg = (RR + nw - 1) / nw;
-	const int lo = warp * seg, hi = min(RR, lo + seg);
-	/* pass 1: faces per warp range */
-	uint32_t cnt = 0;
-	for (int r = lo + lane; r < hi; r += 32) {
-		uint64_t fx, fy, fz;
-		face_bits<RB>(m, r & (R - 1), r >> RB, fx, fy, fz);
-		cnt += __popcll(fx) + __popcll(fy) + __popcll(fz);
-	}
+	/* pass 1: faces per 32-row group */
+	for (int g = warp; g < NG; g += nw) {
+		const int r = g * 32 + lane;
+		uint32_t c = 0;
+		if (r < RR) {
+			uint64_t fx, fy, fz;
+			face_bits<RB>(m, r & (R - 1), r >> RB, fx, fy, fz);
+			c = __popcll(fx) + __popcll(fy) + __popcll(fz);
+		}
 #pragma unroll
-	for (int d = 16; d; d >>= 1) cnt += __shfl_xor_sync(kFull, cnt, d);
-	if (lane == 0) m.wb[warp] = cnt;
-	__syncthreads();
-	if (warp == 0) {
-		const uint32_t v = lane < nw ? m.wb[lane] : 0u;
-		const uint32_t inc = warp_incl_add(v);
-		if (lane < nw) m.wb[lane] = inc - v;
-		if (lane == 31) s_faces = inc;
+		for (int d = 16; d; d >>= 1) c += __shfl_xor_sync(kFull, c, d);
+		if (lane == 0) m.grp[g] = c;
 	}
 	__syncthreads();
-	const uint32_t faces = s_faces;
+	const uint32_t faces = scan_groups(m.grp, NG, m.tmp);
 	if (threadIdx.x == 0) {
 		const uint64_t uv = (uint64_t)faces * 2u;             /* 32 B per face */
 		const uint64_t ui = ((uint64_t)faces * 24u + 15u) / 16u;
@@ -675,6 +748,7 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
 		s_base[0] = bv;
 		s_base[1] = bi;
 		s_ok = ok;
+		s_next = 0;
 		out->vbo_off = bv * 8u;
 		out->ibo_off = bi * 4u;
 		out->vbo_items = faces * 16u;
@@ -688,29 +762,40 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
 	if (!s_ok || faces == 0) return;
 	int16_t *vbo = (int16_t *)avbo.base + s_base[0] * 8u;
 	uint32_t *ibo = (uint32_t *)aibo.base + s_base[1] * 4u;
-	/* pass 2: 32 rows per step, one face per lane */
-	uint32_t base = m.wb[warp];
-	for (int g = lo; g < hi; g += 32) {
-		const int r = g + lane;
+	/* pass 2: warps take 32-row groups from a shared counter; one face per
+	 * lane per step */
+	for (;;) {
+		uint32_t g = 0;
+		if (lane == 0) g = atomicAdd(&s_next, 1u);
+		g = __shfl_sync(kFull, g, 0);
+		if (g >= (uint32_t)NG) break;
+		const int r = (int)g * 32 + lane;
 		uint64_t fx = 0, fy = 0, fz = 0;
-		if (r < hi) face_bits<RB>(m, r & (R - 1), r >> RB, fx, fy, fz);
+		if (r < RR) face_bits<RB>(m, r & (R - 1), r >> RB, fx, fy, fz);
 		const uint32_t c = __popcll(fx) + __popcll(fy) + __popcll(fz);
 		const uint32_t inc = warp_incl_add(c);
 		const uint32_t excl = inc - c;
 		const uint32_t T = __shfl_sync(kFull, inc, 31);
-		for (uint32_t k = 0; k < T; k += 32) {
-			const uint32_t j = k + lane;
-			const int s = search_lane(excl, j);
-			const uint32_t es = __shfl_sync(kFull, excl, s);
-			const uint64_t sx = shfl64(fx, s), sy = shfl64(fy, s), sz = shfl64(fz, s);
-			if (j < T) {
+		const uint32_t base = m.grp[g];
+		for (uint32_t k = 0; k < T; k += 64) {
+			const uint32_t j0 = k + lane, j1 = k + 32 + lane;
+			const int s0 = search_lane(excl, j0), s1 = search_lane(excl, j1);
+			const uint32_t e0 = __shfl_sync(kFull, excl, s0), e1 = __shfl_sync(kFull, excl, s1);
+			const uint64_t ax = shfl64(fx, s0), ay = shfl64(fy, s0), az = shfl64(fz, s0);
+			const uint64_t bx = shfl64(fx, s1), by = shfl64(fy, s1), bz = shfl64(fz, s1);
+			if (j0 < T) {
 				int x, i;
-				select_face<RB>(sx, sy, sz, j - es, x, i);
-				const int rr = g + s;
-				emit_face<RB>(S, stream, m, cv, x, rr & (R - 1), rr >> RB, i, base + j, vbo, ibo);
+				select_face<RB>(ax, ay, az, j0 - e0, x, i);
+				const int rr = (int)g * 32 + s0;
+				emit_face<RB>(S, stream, m, cv, x, rr & (R - 1), rr >> RB, i, base + j0, vbo, ibo);
+			}
+			if (j1 < T) {
+				int x, i;
+				select_face<RB>(bx, by, bz, j1 - e1, x, i);
+				const int rr = (int)g * 32 + s1;
+				emit_face<RB>(S, stream, m, cv, x, rr & (R - 1), rr >> RB, i, base + j1, vbo, ibo);
 			}
 		}
-		base += T;
 	}
 }
 
@@ -764,12 +849,11 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 			    int lod_max, ChunkOut *out, const Arena &asvl)
 {
 	using G = Geo<RB>;
-	constexpr int R = G::R, S1 = G::S;
+	constexpr int R = G::R;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-	__shared__ uint32_t s_cnt[kMaxLevels];
 	__shared__ unsigned long long s_base;
-	__shared__ uint32_t s_ok;
-	int lvoff[kMaxLevels];
+	__shared__ uint32_t s_ok, s_next;
+	int lvoff[kMaxLevels], gfirst[kMaxLevels + 1];
 	{
 		int t = 0;
 		for (int l = 1; l < kMaxLevels; l++) {
@@ -777,7 +861,13 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 			t += ((R >> l) + 1) * ((R >> l) + 1);
 		}
 		lvoff[0] = 0;
+		int g = 0;
+		for (int l = 0; l <= kMaxLevels; l++) {
+			gfirst[l] = g;
+			if (l < kMaxLevels && l <= lod_max) g += G::groups_of(((R >> l) + 1) * ((R >> l) + 1));
+		}
 	}
+	splat_prepare<RB>(m);
 	/* level rows: pairwise OR of the child rows, compacted along x */
 	for (int l = 1; l <= lod_max; l++) {
 		const int n = (R >> l) + 1, np = (R >> (l - 1)) + 1;
@@ -800,78 +890,86 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 		}
 		__syncthreads();
 	}
-	/* pass 1: splats per level per warp range */
-	for (int l = 0; l <= lod_max; l++) {
-		const int n = l ? (R >> l) + 1 : S1;
-		const int seg = (n * n + nw - 1) / nw;
-		const int lo = warp * seg, hi = min(n * n, lo + seg);
+	/* pass 1: splats per 32-row group, levels in order */
+	const int ngroups = gfirst[lod_max + 1];
+	for (int g = warp; g < ngroups; g += nw) {
+		int l = 0;
+		while (g >= gfirst[l + 1]) l++;
+		const int n = (R >> l) + 1;
+		const int r = (g - gfirst[l]) * 32 + lane;
 		uint32_t c = 0;
-		for (int i = lo + lane; i < hi; i += 32) {
+		if (r < n * n) {
 			uint32_t xr;
-			c += __popcll(level_row<RB>(m, lvoff, l, i % n, i / n, xr)) + xr;
+			c = __popcll(level_row<RB>(m, lvoff, l, r % n, r / n, xr)) + xr;
 		}
 #pragma unroll
 		for (int d = 16; d; d >>= 1) c += __shfl_xor_sync(kFull, c, d);
-		if (lane == 0) m.wb[l * 16 + warp] = c;
+		if (lane == 0) m.grp[g] = c;
 	}
 	__syncthreads();
-	if (warp == 0) {
-		uint32_t level_base = 0;
-		for (int l = 0; l <= lod_max; l++) {
-			const uint32_t v = lane < nw ? m.wb[l * 16 + lane] : 0u;
-			const uint32_t inc = warp_incl_add(v);
-			if (lane < nw) m.wb[l * 16 + lane] = level_base + inc - v;
-			const uint32_t tot = __shfl_sync(kFull, inc, 31);
-			if (lane == 0) s_cnt[l] = tot;
-			level_base += tot;
+	const uint32_t total = scan_groups(m.grp, ngroups, m.tmp);
+	if (threadIdx.x == 0) {
+		const uint64_t units = ((uint64_t)total + 1u) / 2u; /* 8 B per splat */
+		unsigned long long b = units ? atomicAdd(asvl.cursor, (unsigned long long)units) : 0ull;
+		const uint32_t ok = (b + units <= asvl.cap_units);
+		s_base = b;
+		s_ok = ok;
+		s_next = 0;
+		out->svl_off = b * 8u;
+		out->svl_total = total * 4u;
+		for (int l = 0; l < kMaxLevels; l++) {
+			uint32_t c = 0;
+			if (l <= lod_max) {
+				const uint32_t b0 = m.grp[gfirst[l]];
+				const uint32_t b1 = gfirst[l + 1] < ngroups ? m.grp[gfirst[l + 1]] : total;
+				c = b1 - b0;
+			}
+			out->svl_items[l] = c * 4u;
 		}
-		if (lane == 0) {
-			const uint32_t total = level_base;
-			const uint64_t units = ((uint64_t)total + 1u) / 2u; /* 8 B per splat */
-			unsigned long long b = units ? atomicAdd(asvl.cursor, (unsigned long long)units) : 0ull;
-			const uint32_t ok = (b + units <= asvl.cap_units);
-			s_base = b;
-			s_ok = ok;
-			out->svl_off = b * 8u;
-			out->svl_total = total * 4u;
-			for (int l = 0; l < kMaxLevels; l++) out->svl_items[l] = l <= lod_max ? s_cnt[l] * 4u : 0u;
-			out->vbo_off = out->ibo_off = 0;
-			out->vbo_items = out->ibo_items = 0;
-			out->status = ok ? 0u : kStatusOverflow;
-		}
+		out->vbo_off = out->ibo_off = 0;
+		out->vbo_items = out->ibo_items = 0;
+		out->status = ok ? 0u : kStatusOverflow;
 	}
 	__syncthreads();
 	if (!s_ok) return;
 	int16_t *dst = (int16_t *)asvl.base + s_base * 8u;
-	/* pass 2: 32 rows per step, one splat per lane */
-	for (int l = 0; l <= lod_max; l++) {
-		const int n = l ? (R >> l) + 1 : S1;
-		const int seg = (n * n + nw - 1) / nw;
-		const int lo = warp * seg, hi = min(n * n, lo + seg);
-		uint32_t base = m.wb[l * 16 + warp];
-		for (int g = lo; g < hi; g += 32) {
-			const int r = g + lane;
-			uint64_t row = 0;
-			uint32_t xr = 0;
-			if (r < hi) row = level_row<RB>(m, lvoff, l, r % n, r / n, xr);
-			const uint32_t c = __popcll(row) + xr;
-			const uint32_t inc = warp_incl_add(c);
-			const uint32_t excl = inc - c;
-			const uint32_t T = __shfl_sync(kFull, inc, 31);
-			for (uint32_t k = 0; k < T; k += 32) {
-				const uint32_t j = k + lane;
-				const int s = search_lane(excl, j);
-				const uint32_t es = __shfl_sync(kFull, excl, s);
-				const uint64_t srow = shfl64(row, s);
-				if (j < T) {
-					const int kk = (int)(j - es);
-					const int x = kk < __popcll(srow) ? select_bit(srow, kk) : R;
-					const int rr = g + s;
-					emit_splat<RB>(S, stream, m, cv, lvoff, l, x, rr % n, rr / n,
-						       dst + (size_t)(base + j) * 4);
-				}
+	/* pass 2: warps take groups from a shared counter; one splat per lane */
+	for (;;) {
+		uint32_t g = 0;
+		if (lane == 0) g = atomicAdd(&s_next, 1u);
+		g = __shfl_sync(kFull, g, 0);
+		if (g >= (uint32_t)ngroups) break;
+		int l = 0;
+		while ((int)g >= gfirst[l + 1]) l++;
+		const int n = (R >> l) + 1;
+		const int r0 = ((int)g - gfirst[l]) * 32;
+		const int r = r0 + lane;
+		uint64_t row = 0;
+		uint32_t xr = 0;
+		if (r < n * n) row = level_row<RB>(m, lvoff, l, r % n, r / n, xr);
+		const uint32_t c = __popcll(row) + xr;
+		const uint32_t inc = warp_incl_add(c);
+		const uint32_t excl = inc - c;
+		const uint32_t T = __shfl_sync(kFull, inc, 31);
+		const uint32_t base = m.grp[g];
+		/* two items per lane per step keep twice the loads in flight */
+		for (uint32_t k = 0; k < T; k += 64) {
+			const uint32_t j0 = k + lane, j1 = k + 32 + lane;
+			const int s0 = search_lane(excl, j0), s1 = search_lane(excl, j1);
+			const uint32_t e0 = __shfl_sync(kFull, excl, s0), e1 = __shfl_sync(kFull, excl, s1);
+			const uint64_t w0 = shfl64(row, s0), w1 = shfl64(row, s1);
+			if (j0 < T) {
+				const int k0 = (int)(j0 - e0);
+				const int x0 = k0 < __popcll(w0) ? select_bit(w0, k0) : R;
+				const int r0_ = r0 + s0;
+				emit_splat<RB>(S, stream, m, cv, lvoff, l, x0, r0_ % n, r0_ / n, dst + (size_t)(base + j0) * 4);
 			}
-			base += T;
+			if (j1 < T) {
+				const int k1 = (int)(j1 - e1);
+				const int x1 = k1 < __popcll(w1) ? select_bit(w1, k1) : R;
+				const int r1_ = r0 + s1;
+				emit_splat<RB>(S, stream, m, cv, lvoff, l, x1, r1_ % n, r1_ / n, dst + (size_t)(base + j1) * 4);
+			}
 		}
 	}
 }
@@ -895,7 +993,7 @@ __global__ void __launch_bounds__(512, 2) k_geometry(const SetDesc *__restrict__
 		next = nitems;
 		const WorkItem wi = items[it];
 		const SetDesc S = sets[wi.set];
-		ChunkOut *out = outs + it;
+		ChunkOut *out = outs + wi.slot;
 		uint32_t cv[3];
 		chunk_coords(S, wi.chunk, cv);
 		const uint32_t N = (uint32_t)R * R * R;
