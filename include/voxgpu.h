@@ -66,6 +66,8 @@ typedef struct vp_chunk_result {
 
 /* Rebuild flags */
 #define VP_REBUILD_PERSISTENT 1u /* persistent CTAs + device work queue */
+#define VP_REBUILD_PLAIN 2u      /* one launch per chunk and pass (comparison path) */
+#define VP_REBUILD_GROUP 4u      /* also build the LOD/octree draw groups */
 
 VP_API const char *vp_strerror(int code);
 VP_API const char *vp_last_cuda_error(void);
@@ -102,6 +104,27 @@ VP_API int vp_world_results(vp_world *w, vp_chunk_result *out, uint32_t n);
 VP_API int vp_world_read_svl(vp_world *w, uint64_t off, uint64_t n, int16_t *dst);
 VP_API int vp_world_read_vbo(vp_world *w, uint64_t off, uint64_t n, int16_t *dst);
 VP_API int vp_world_read_ibo(vp_world *w, uint64_t off, uint64_t n, uint32_t *dst);
+
+/* LOD/octree draw groups of the last rebuild made with VP_REBUILD_GROUP
+ * (gfx_update_svl, src/gfx/vsplat.c:209-331, minus the GL upload): for LOD
+ * `lod`, node i (numbered flatten3(node, max_bitw - min(lod, max_bitw)))
+ * holds the concatenated level-`lod` splats of its member chunks, scanned x
+ * outer, y, z inner; off[i] / items[i] locate it in the group arena, in
+ * int16 units. n = number of nodes to read (at most the chunk count). */
+VP_API int vp_world_group_nodes(vp_world *w, int lod, uint64_t *off, uint32_t *items, uint32_t n);
+VP_API int vp_world_read_group(vp_world *w, uint64_t off, uint64_t n, int16_t *dst);
+
+/* RLE codec on host buffers (the device does the work). vp_rle_encode is
+ * rle_compress (src/chunkset/rle.c:44-87): out receives the stream
+ * including its 0 terminator, *out_len its word count; lengths below
+ * 0xFFFFFF. vp_rle_decode is rle_decompress (src/chunkset/rle.c:90-117):
+ * the first word is always consumed, decoding stops at the first 0 word;
+ * *out_len receives the voxel count. VP_EOVERFLOW when out_cap is short
+ * (*out_len then holds the size needed). */
+VP_API int vp_rle_encode(vp_ctx *ctx, const uint8_t *vox, uint32_t length, uint32_t *out, uint32_t out_cap,
+			 uint32_t *out_len);
+VP_API int vp_rle_decode(vp_ctx *ctx, const uint32_t *words, uint32_t nwords, uint8_t *out, uint32_t out_cap,
+			 uint32_t *out_len);
 
 /* Kernel timing: with timing on, every rebuild records CUDA events around
  * its kernels on the context stream; vp_world_kernel_ms returns the summed

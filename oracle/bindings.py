@@ -152,6 +152,20 @@ class OracleWorld(_Base):
         return self.lib.vpo_rebuild(self.h, _vp(chunks), len(chunks), _vp(mm) if mm is not None else None,
                                     lod_max, nthreads)
 
+    def group_node(self, lod, node, svl_lists, svl_items):
+        """gfx_update_svl's concatenation for one node (oracle/vpo.c)."""
+        n = self.nchunks
+        keep = [np.ascontiguousarray(a, np.int16) for a in svl_lists]
+        its = [np.ascontiguousarray(a, np.uint32) for a in svl_items]
+        P16 = (ctypes.c_void_p * n)(*[a.ctypes.data if len(a) else 0 for a in keep])
+        P32 = (ctypes.c_void_p * n)(*[a.ctypes.data for a in its])
+        total = sum(int(a[lod]) for a in its)
+        out = np.zeros(max(total, 1), np.int16)
+        nd = np.asarray(node, np.uint32)
+        m = self.lib.vpo_group_node(self.h, lod, _vp(nd), ctypes.cast(P16, ctypes.c_void_p),
+                                    ctypes.cast(P32, ctypes.c_void_p), _vp(out))
+        return out[:m].copy()
+
     def mask(self, c):
         m = np.zeros((self.R + 1) ** 3, np.uint8)
         self.lib.vpo_make_mask(self.h, c, _vp(m))

@@ -4,6 +4,8 @@
  */
 #include "voxgpu.h"
 #include "vp_geometry.h"
+#include "vp_rle.h"
+#include "vp_group.h"
 
 #include <algorithm>
 #include <cstdio>
@@ -56,6 +58,12 @@ struct vp_ctx {
 	cudaStream_t stream;
 	int timing;
 	int sm_count;
+	/* staging for the host-buffer codec calls */
+	uint8_t *d_bytes = nullptr;
+	size_t bytes_cap = 0;
+	uint32_t *d_words = nullptr;
+	size_t words_cap = 0;
+	uint64_t *d_scalars = nullptr; /* [0] cursor, [1] off, [2] len|status */
 };
 
 struct vp_world {
@@ -85,6 +93,12 @@ struct vp_world {
 	int last_lod = 4;
 	unsigned last_flags = 0;
 	bool uploaded = false;
+	/* grouping */
+	uint64_t *d_gcounts = nullptr, *d_gtotal = nullptr, *d_node_off = nullptr;
+	uint32_t *d_node_items = nullptr;
+	int16_t *d_garena = nullptr;
+	uint64_t garena_units = 0;
+	int grouped_lod = -1;
 	std::vector<cudaEvent_t> ev;             /* pairs per kernel */
 	std::vector<int> ev_kind;                /* 0 shell, 1 geometry */
 	double ms[2] = {0, 0};
@@ -133,8 +147,96 @@ VP_API void vp_ctx_destroy(vp_ctx *c)
 	if (!c) return;
 	cudaSetDevice(c->device);
 	cudaStreamSynchronize(c->stream);
+	dev_free(c->d_bytes);
+	dev_free(c->d_words);
+	dev_free(c->d_scalars);
 	cudaStreamDestroy(c->stream);
 	delete c;
+}
+
+static int ensure_stage(vp_ctx *c, size_t nbytes, size_t nwords)
+{
+	if (nbytes > c->bytes_cap) {
+		dev_free(c->d_bytes);
+		c->bytes_cap = 0;
+		int rc = dev_alloc(&c->d_bytes, nbytes);
+		if (rc) return rc;
+		c->bytes_cap = nbytes;
+	}
+	if (nwords > c->words_cap) {
+		dev_free(c->d_words);
+		c->words_cap = 0;
+		int rc = dev_alloc(&c->d_words, nwords);
+		if (rc) return rc;
+		c->words_cap = nwords;
+	}
+	if (!c->d_scalars) {
+		int rc = dev_alloc(&c->d_scalars, 4);
+		if (rc) return rc;
+	}
+	return VP_OK;
+}
+
+VP_API int vp_rle_encode(vp_ctx *c, const uint8_t *vox, uint32_t length, uint32_t *out, uint32_t out_cap,
+			 uint32_t *out_len)
+{
+	if (!c || !vox || !out || !out_len || length == 0) return VP_EINVAL;
+	if (length >= 0xFFFFFFu) return VP_EUNSUPPORTED;
+	CK(cudaSetDevice(c->device));
+	const size_t padded = ((size_t)length + 15u) & ~(size_t)15u;
+	int rc = ensure_stage(c, padded, (size_t)length + 8u);
+	if (rc) return rc;
+	cudaStream_t st = c->stream;
+	CK(cudaMemcpyAsync(c->d_bytes, vox, length, cudaMemcpyHostToDevice, st));
+	CK(cudaMemsetAsync(c->d_scalars, 0, 4 * sizeof(uint64_t), st));
+	cudaError_t e = launch_rle_encode(c->d_bytes, 1, length, c->d_words, c->words_cap,
+					  (unsigned long long *)c->d_scalars, c->d_scalars + 1,
+					  (uint32_t *)(c->d_scalars + 2), (uint32_t *)(c->d_scalars + 3), st);
+	if (e != cudaSuccess) return cuda_fail(e, "rle encode launch");
+	uint64_t sc[4];
+	CK(cudaMemcpyAsync(sc, c->d_scalars, sizeof(sc), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	const uint32_t n = (uint32_t)sc[2];
+	if ((uint32_t)sc[3] & kStatusOverflow) return VP_EOVERFLOW;
+	*out_len = n;
+	if (n > out_cap) return VP_EOVERFLOW;
+	CK(cudaMemcpyAsync(out, c->d_words + sc[1], (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	return VP_OK;
+}
+
+VP_API int vp_rle_decode(vp_ctx *c, const uint32_t *words, uint32_t nwords, uint8_t *out, uint32_t out_cap,
+			 uint32_t *out_len)
+{
+	if (!c || !words || !out || !out_len || nwords == 0) return VP_EINVAL;
+	/* the reference consumes the first word, then stops at the first 0 */
+	uint32_t n = 1;
+	uint64_t total = words[0] & 0xFFFFFFu;
+	while (n < nwords && words[n]) {
+		total += words[n] & 0xFFFFFFu;
+		n++;
+	}
+	if (n >= nwords && nwords > 1 && words[nwords - 1] != 0) return VP_EINVAL; /* no terminator */
+	*out_len = (uint32_t)total;
+	if (total > out_cap) return VP_EOVERFLOW;
+	if (total == 0) return VP_OK;
+	CK(cudaSetDevice(c->device));
+	int rc = ensure_stage(c, (total + 15u) & ~(uint64_t)15u, (size_t)n + 9u);
+	if (rc) return rc;
+	cudaStream_t st = c->stream;
+	CK(cudaMemsetAsync(c->d_words, 0, ((size_t)n + 9u) * sizeof(uint32_t), st));
+	CK(cudaMemcpyAsync(c->d_words, words, (size_t)n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+	const uint64_t off0 = 0;
+	const uint32_t len0 = n + 1u; /* runs + terminator */
+	CK(cudaMemcpyAsync(c->d_scalars, &off0, sizeof(off0), cudaMemcpyHostToDevice, st));
+	CK(cudaMemcpyAsync(c->d_scalars + 1, &len0, sizeof(len0), cudaMemcpyHostToDevice, st));
+	CK(cudaMemsetAsync(c->d_scalars + 2, 0, sizeof(uint64_t), st));
+	cudaError_t e = launch_rle_decode_bytes(c->d_words, c->d_scalars, (const uint32_t *)(c->d_scalars + 1), nullptr,
+						1, (uint32_t)total, c->d_bytes, (uint32_t *)(c->d_scalars + 2), st);
+	if (e != cudaSuccess) return cuda_fail(e, "rle decode launch");
+	CK(cudaMemcpyAsync(out, c->d_bytes, total, cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	return VP_OK;
 }
 
 VP_API void *vp_ctx_stream(vp_ctx *c) { return c ? (void *)c->stream : nullptr; }
@@ -199,6 +301,11 @@ VP_API void vp_world_destroy(vp_world *w)
 	dev_free(w->d_queue);
 	dev_free(w->d_cursors);
 	for (int a = 0; a < 3; a++) dev_free(w->d_arena[a]);
+	dev_free(w->d_gcounts);
+	dev_free(w->d_gtotal);
+	dev_free(w->d_node_off);
+	dev_free(w->d_node_items);
+	dev_free(w->d_garena);
 	for (cudaEvent_t e : w->ev) cudaEventDestroy(e);
 	delete w;
 }
@@ -326,6 +433,38 @@ static int ensure_arenas(vp_world *w)
 	return VP_OK;
 }
 
+static int enqueue_group(vp_world *w, int lod_max)
+{
+	cudaStream_t st = w->ctx->stream;
+	const size_t L = (size_t)VP_MAX_LEVELS, n = w->nchunks;
+	int rc;
+	if (!w->d_gcounts) {
+		if ((rc = dev_alloc(&w->d_gcounts, L * n)) || (rc = dev_alloc(&w->d_gtotal, L)) ||
+		    (rc = dev_alloc(&w->d_node_off, L * n)) || (rc = dev_alloc(&w->d_node_items, L * n)))
+			return rc;
+	}
+	if (w->garena_units < w->cap[0]) {
+		dev_free(w->d_garena);
+		w->garena_units = 0;
+		if ((rc = dev_alloc(&w->d_garena, (size_t)w->cap[0] * 8u))) return rc;
+		w->garena_units = w->cap[0];
+	}
+	CK(cudaMemsetAsync(w->d_node_items, 0, L * n * sizeof(uint32_t), st));
+	GroupArgs a;
+	for (int i = 0; i < 3; i++) a.max_bitw[i] = (uint32_t)w->max_bitw[i];
+	a.counts = w->d_gcounts;
+	a.level_total = w->d_gtotal;
+	a.node_off = w->d_node_off;
+	a.node_items = w->d_node_items;
+	a.svl = (const int16_t *)w->d_arena[0];
+	a.out = w->d_garena;
+	cudaError_t e = launch_group(w->d_outs, w->nchunks, lod_max, a, st);
+	if (e != cudaSuccess) return cuda_fail(e, "group launch");
+	w->launches += 3;
+	w->grouped_lod = lod_max;
+	return VP_OK;
+}
+
 static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 {
 	vp_ctx *ctx = w->ctx;
@@ -362,24 +501,53 @@ static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 		cudaEventCreate(&e2);
 		cudaEventRecord(e0, st);
 	}
-	/* shell pass */
-	L.run_shell = 1;
-	GeoLaunch Ls = L;
-	Ls.n_items = 0;
-	cudaError_t e = launch_geometry(w->root_bitw, Ls, st);
-	if (e != cudaSuccess) return cuda_fail(e, "shell launch");
-	if (ctx->timing) cudaEventRecord(e1, st);
-	GeoLaunch Lg = L;
-	Lg.run_shell = 0;
-	e = launch_geometry(w->root_bitw, Lg, st);
-	if (e != cudaSuccess) return cuda_fail(e, "geometry launch");
+	cudaError_t e = cudaSuccess;
+	if (flags & VP_REBUILD_PLAIN) {
+		/* one launch per chunk and pass: every shell, then every chunk's
+		 * geometry (a chunk reads its neighbours' shells) */
+		for (uint32_t k = 0; k < w->nchunks && e == cudaSuccess; k++) {
+			GeoLaunch Ls = L;
+			Ls.n_items = 0;
+			Ls.shell_items = w->d_items + k;
+			Ls.n_shell = 1;
+			Ls.run_shell = 1;
+			e = launch_geometry(w->root_bitw, Ls, st);
+		}
+		if (ctx->timing) cudaEventRecord(e1, st);
+		for (uint32_t k = 0; k < w->nchunks && e == cudaSuccess; k++) {
+			GeoLaunch Lg = L;
+			Lg.run_shell = 0;
+			Lg.items = w->d_items + k;
+			Lg.n_items = 1;
+			Lg.queue = nullptr;
+			e = launch_geometry(w->root_bitw, Lg, st);
+		}
+		if (e != cudaSuccess) return cuda_fail(e, "plain launches");
+		w->launches += 2 * w->nchunks;
+	} else {
+		L.run_shell = 1;
+		GeoLaunch Ls = L;
+		Ls.n_items = 0;
+		e = launch_geometry(w->root_bitw, Ls, st);
+		if (e != cudaSuccess) return cuda_fail(e, "shell launch");
+		if (ctx->timing) cudaEventRecord(e1, st);
+		GeoLaunch Lg = L;
+		Lg.run_shell = 0;
+		e = launch_geometry(w->root_bitw, Lg, st);
+		if (e != cudaSuccess) return cuda_fail(e, "geometry launch");
+		w->launches += 2;
+	}
 	if (ctx->timing) {
 		cudaEventRecord(e2, st);
 		w->ev.push_back(e0);
 		w->ev.push_back(e1);
 		w->ev.push_back(e2);
 	}
-	w->launches += 2;
+	w->grouped_lod = -1;
+	if (flags & VP_REBUILD_GROUP) {
+		int rc2 = enqueue_group(w, lod_max);
+		if (rc2) return rc2;
+	}
 	w->last_lod = lod_max;
 	w->last_flags = flags;
 	return VP_OK;
@@ -454,6 +622,29 @@ VP_API int vp_world_read_vbo(vp_world *w, uint64_t off, uint64_t n, int16_t *dst
 VP_API int vp_world_read_ibo(vp_world *w, uint64_t off, uint64_t n, uint32_t *dst)
 {
 	return read_arena(w, 2, off * 4u, n * 4u, dst);
+}
+
+VP_API int vp_world_group_nodes(vp_world *w, int lod, uint64_t *off, uint32_t *items, uint32_t n)
+{
+	if (!w || lod < 0 || lod > w->grouped_lod || !off || !items) return VP_EINVAL;
+	if (n > w->nchunks) n = w->nchunks;
+	cudaStream_t st = w->ctx->stream;
+	CK(cudaMemcpyAsync(off, w->d_node_off + (size_t)lod * w->nchunks, (size_t)n * sizeof(uint64_t),
+			   cudaMemcpyDeviceToHost, st));
+	CK(cudaMemcpyAsync(items, w->d_node_items + (size_t)lod * w->nchunks, (size_t)n * sizeof(uint32_t),
+			   cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	return VP_OK;
+}
+
+VP_API int vp_world_read_group(vp_world *w, uint64_t off, uint64_t n, int16_t *dst)
+{
+	if (!w || (!dst && n) || !w->d_garena) return VP_EINVAL;
+	if ((off + n) * 2u > w->garena_units * 16u) return VP_EINVAL;
+	if (!n) return VP_OK;
+	CK(cudaMemcpyAsync(dst, w->d_garena + off, n * 2u, cudaMemcpyDeviceToHost, w->ctx->stream));
+	CK(cudaStreamSynchronize(w->ctx->stream));
+	return VP_OK;
 }
 
 VP_API int vp_world_kernel_ms(vp_world *w, double *shell_ms, double *geometry_ms, uint32_t *launches)

@@ -1,0 +1,149 @@
+/*
+ * vp_group.cu — LOD/octree grouping of the splat lists (gfx_update_svl,
+ * src/gfx/vsplat.c:209-331, without the GL upload).
+ *
+ * For LOD l, chunk c belongs to octree node offset >> l, whose members are
+ * the chunks [node << l, min((node+1) << l, max)) scanned x outer, y, z
+ * inner; the node's buffer is the concatenation of its members' level-l
+ * splat segments in that order. Nodes are numbered flatten3(node,
+ * max_bitw - min(l, max_bitw)) as in the reference.
+ *
+ * With power-of-two chunk counts every node is full, so
+ *   key(c) = node_index(c) * members + member_rank(c)
+ * is a bijection onto [0, nchunks): the prefix sum of the level-l item
+ * counts in key order gives every segment's destination, and node i's
+ * buffer starts at the prefix of its first key. One pass scatters counts
+ * into key order, one CTA per level scans them, and a warp per chunk copies
+ * its segment with 8-byte vector moves (one splat per lane).
+ */
+#include "vp_dev.cuh"
+#include "vp_group.h"
+
+namespace vp {
+
+struct GroupGeom {
+	uint32_t mb[3];   /* chunk count exponents */
+	uint32_t eb[3];   /* member extent exponents: min(l, mb) */
+	uint32_t ob[3];   /* node count exponents: mb - eb */
+};
+
+__device__ __forceinline__ GroupGeom group_geom(const uint32_t mb[3], int l)
+{
+	GroupGeom g;
+	for (int i = 0; i < 3; i++) {
+		g.mb[i] = mb[i];
+		g.eb[i] = min((uint32_t)l, mb[i]);
+		g.ob[i] = mb[i] - g.eb[i];
+	}
+	return g;
+}
+
+__device__ __forceinline__ uint32_t group_key(const GroupGeom &g, uint32_t c, uint32_t *node_index, uint32_t *rank)
+{
+	const uint32_t x = c & ((1u << g.mb[0]) - 1u);
+	const uint32_t y = (c >> g.mb[0]) & ((1u << g.mb[1]) - 1u);
+	const uint32_t z = c >> (g.mb[0] + g.mb[1]);
+	const uint32_t nx = x >> g.eb[0], ny = y >> g.eb[1], nz = z >> g.eb[2];
+	const uint32_t lx = x & ((1u << g.eb[0]) - 1u), ly = y & ((1u << g.eb[1]) - 1u), lz = z & ((1u << g.eb[2]) - 1u);
+	*node_index = ((nz << g.ob[1] | ny) << g.ob[0]) | nx; /* flatten3 */
+	*rank = ((lx << g.eb[1] | ly) << g.eb[2]) | lz;       /* x outer, z inner */
+	return (*node_index << (g.eb[0] + g.eb[1] + g.eb[2])) | *rank;
+}
+
+/* counts[l][key(c)] = level-l splat items of chunk c (int16 units) */
+__global__ void k_group_scatter(const ChunkOut *__restrict__ outs, uint32_t nchunks, GroupArgs a)
+{
+	const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+	const int l = blockIdx.y;
+	if (c >= nchunks) return;
+	const GroupGeom g = group_geom(a.max_bitw, l);
+	uint32_t node, rank;
+	const uint32_t key = group_key(g, c, &node, &rank);
+	a.counts[(size_t)l * nchunks + key] = outs[c].svl_items[l];
+}
+
+/* exclusive prefix sum of each level's counts, one CTA per level */
+__global__ void __launch_bounds__(1024) k_group_scan(uint32_t n, GroupArgs a)
+{
+	__shared__ uint64_t wsum[32];
+	__shared__ uint64_t wexcl[32];
+	__shared__ uint64_t s_tile, s_carry;
+	uint64_t *v = a.counts + (size_t)blockIdx.x * n;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	if (threadIdx.x == 0) s_carry = 0;
+	__syncthreads();
+	for (uint32_t base = 0; base < n; base += blockDim.x) {
+		const uint32_t i = base + threadIdx.x;
+		const uint64_t x = i < n ? v[i] : 0ull;
+		uint64_t inc = x;
+#pragma unroll
+		for (int d = 1; d < 32; d <<= 1) {
+			const uint64_t t = __shfl_up_sync(kFull, inc, d);
+			if (lane >= d) inc += t;
+		}
+		if (lane == 31) wsum[warp] = inc;
+		__syncthreads();
+		if (warp == 0) {
+			const uint64_t w = lane < nw ? wsum[lane] : 0ull;
+			uint64_t wi = w;
+#pragma unroll
+			for (int d = 1; d < 32; d <<= 1) {
+				const uint64_t t = __shfl_up_sync(kFull, wi, d);
+				if (lane >= d) wi += t;
+			}
+			wexcl[lane] = wi - w;
+			if (lane == 31) s_tile = wi;
+		}
+		__syncthreads();
+		if (i < n) v[i] = s_carry + wexcl[warp] + inc - x;
+		__syncthreads();
+		if (threadIdx.x == 0) s_carry += s_tile;
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) a.level_total[blockIdx.x] = s_carry;
+}
+
+/* one warp per chunk: copy its level-l segment; the first member of each
+ * node also records the node's offset and length */
+__global__ void k_group_copy(const ChunkOut *__restrict__ outs, uint32_t nchunks, GroupArgs a)
+{
+	const uint32_t warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const int lane = threadIdx.x & 31;
+	const int l = blockIdx.y;
+	const uint32_t c = warp_global;
+	if (c >= nchunks) return;
+	const GroupGeom g = group_geom(a.max_bitw, l);
+	uint32_t node, rank;
+	const uint32_t key = group_key(g, c, &node, &rank);
+	uint64_t lbase = 0;
+	for (int k = 0; k < l; k++) lbase += a.level_total[k];
+	const uint64_t *cnt = a.counts + (size_t)l * nchunks;
+	const uint64_t dst_off = lbase + cnt[key];
+	if (rank == 0 && lane == 0) {
+		const uint32_t mbits = g.eb[0] + g.eb[1] + g.eb[2];
+		const uint32_t next_key = (node + 1u) << mbits;
+		const uint64_t end = next_key < nchunks ? cnt[next_key] : a.level_total[l];
+		a.node_off[(size_t)l * nchunks + node] = dst_off;
+		a.node_items[(size_t)l * nchunks + node] = (uint32_t)(end - cnt[key]);
+	}
+	const ChunkOut o = outs[c];
+	const uint32_t items = o.svl_items[l];
+	if (!items) return;
+	uint64_t src_off = o.svl_off;
+	for (int k = 0; k < l; k++) src_off += o.svl_items[k];
+	const uint2 *src = (const uint2 *)(a.svl + src_off);
+	uint2 *dst = (uint2 *)(a.out + dst_off);
+	for (uint32_t s = lane; s < items / 4u; s += 32u) dst[s] = src[s];
+}
+
+cudaError_t launch_group(const ChunkOut *outs, uint32_t nchunks, int lod_max, const GroupArgs &a, cudaStream_t st)
+{
+	if (!nchunks) return cudaSuccess;
+	const int L = lod_max + 1;
+	k_group_scatter<<<dim3((nchunks + 255) / 256, L), 256, 0, st>>>(outs, nchunks, a);
+	k_group_scan<<<L, 1024, 0, st>>>(nchunks, a);
+	k_group_copy<<<dim3((nchunks * 32u + 255u) / 256u, L), 256, 0, st>>>(outs, nchunks, a);
+	return cudaGetLastError();
+}
+
+} // namespace vp

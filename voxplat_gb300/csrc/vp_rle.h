@@ -1,0 +1,21 @@
+/* vp_rle.h — launch interface of the RLE codec kernels. */
+#pragma once
+#include "vp_dev.cuh"
+
+namespace vp {
+
+/* Encode nchunks voxel volumes of N bytes (contiguous, 16-byte aligned and
+ * padded) into streams bump-allocated from `pool` (cap_words, cursor);
+ * out_off/out_len per chunk; *status gets kStatusOverflow on lack of room. */
+cudaError_t launch_rle_encode(const uint8_t *vox, uint32_t nchunks, uint32_t N, uint32_t *pool, uint64_t cap_words,
+			      unsigned long long *cursor, uint64_t *out_off, uint32_t *out_len, uint32_t *status,
+			      cudaStream_t st);
+
+/* Decode the streams of `chunks` (or 0..n-1 when chunks is NULL) into
+ * consecutive N-byte volumes; *status gets kStatusBadStream when a stream
+ * does not cover exactly N voxels. */
+cudaError_t launch_rle_decode_bytes(const uint32_t *pool, const uint64_t *off, const uint32_t *len,
+				    const uint32_t *chunks, uint32_t n, uint32_t N, uint8_t *vox, uint32_t *status,
+				    cudaStream_t st);
+
+} // namespace vp

@@ -13,6 +13,8 @@ from . import build as _build
 VP_OK = 0
 VP_MAX_LEVELS = 8
 VP_REBUILD_PERSISTENT = 1
+VP_REBUILD_PLAIN = 2
+VP_REBUILD_GROUP = 4
 
 
 class VoxGpuError(RuntimeError):
@@ -79,6 +81,10 @@ def load(build_if_missing=True):
         "vp_world_read_svl": (I, [V, U64, U64, V]),
         "vp_world_read_vbo": (I, [V, U64, U64, V]),
         "vp_world_read_ibo": (I, [V, U64, U64, V]),
+        "vp_world_group_nodes": (I, [V, I, V, V, U32]),
+        "vp_world_read_group": (I, [V, U64, U64, V]),
+        "vp_rle_encode": (I, [V, V, U32, V, U32, ctypes.POINTER(U32)]),
+        "vp_rle_decode": (I, [V, V, U32, V, U32, ctypes.POINTER(U32)]),
         "vp_world_kernel_ms": (I, [V, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                    ctypes.POINTER(U32)]),
     }
@@ -126,6 +132,25 @@ class Context:
     def sync(self):
         check(self.lib.vp_ctx_sync(self.h), "vp_ctx_sync")
 
+    def rle_encode(self, vox):
+        """rle_compress on the device: the stream incl. its 0 terminator."""
+        vox = np.ascontiguousarray(vox, dtype=np.uint8)
+        out = np.zeros(len(vox) + 2, np.uint32)
+        n = ctypes.c_uint32()
+        check(self.lib.vp_rle_encode(self.h, _p(vox), len(vox), _p(out), len(out), ctypes.byref(n)), "vp_rle_encode")
+        return out[:n.value].copy()
+
+    def rle_decode(self, words, cap=None):
+        """rle_decompress on the device."""
+        words = np.ascontiguousarray(words, dtype=np.uint32)
+        if cap is None:
+            cap = int((words & 0xFFFFFF).astype(np.int64).sum())
+        out = np.zeros(max(cap, 1), np.uint8)
+        n = ctypes.c_uint32()
+        check(self.lib.vp_rle_decode(self.h, _p(words), len(words), _p(out), len(out), ctypes.byref(n)),
+              "vp_rle_decode")
+        return out[:n.value].copy()
+
     def set_timing(self, on):
         check(self.lib.vp_ctx_set_timing(self.h, 1 if on else 0), "vp_ctx_set_timing")
 
@@ -167,9 +192,22 @@ class DeviceWorld:
             assert len(m) == self.nchunks
             check(self.lib.vp_world_set_modes(self.h, _p(m)), "vp_world_set_modes")
 
-    def rebuild(self, lod_max=4, persistent=True):
-        flags = VP_REBUILD_PERSISTENT if persistent else 0
+    def rebuild(self, lod_max=4, persistent=True, plain=False, group=False):
+        flags = (VP_REBUILD_PERSISTENT if persistent else 0) | (VP_REBUILD_PLAIN if plain else 0) \
+            | (VP_REBUILD_GROUP if group else 0)
         check(self.lib.vp_world_rebuild(self.h, lod_max, flags), "vp_world_rebuild")
+
+    def group_nodes(self, lod):
+        """(offsets, items) of every octree node of LOD `lod` (int16 units)."""
+        off = np.zeros(self.nchunks, np.uint64)
+        items = np.zeros(self.nchunks, np.uint32)
+        check(self.lib.vp_world_group_nodes(self.h, lod, _p(off), _p(items), self.nchunks), "vp_world_group_nodes")
+        return off, items
+
+    def read_group(self, off, n):
+        out = np.zeros(int(n), np.int16)
+        check(self.lib.vp_world_read_group(self.h, int(off), int(n), _p(out)), "vp_world_read_group")
+        return out
 
     def finish(self):
         check(self.lib.vp_world_finish(self.h), "vp_world_finish")
