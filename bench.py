@@ -182,7 +182,7 @@ def run_ours(args):
     stream = torch.cuda.ExternalStream(ctx.stream)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda:%d" % dev)
     for _ in range(max(args.warmup, 3)):
-        dw.rebuild(LOD_MAX)
+        dw.rebuild(LOD_MAX, group=True)
         dw.finish()
     res = dw.results()
     assert (res["status"] == 0).all()
@@ -198,13 +198,13 @@ def run_ours(args):
             with torch.cuda.stream(stream):
                 flush.zero_()
                 starts[k].record(stream)
-            dw.rebuild(LOD_MAX)
+            dw.rebuild(LOD_MAX, group=True)
             with torch.cuda.stream(stream):
                 ends[k].record(stream)
         ctx.sync()
         torch.cuda.synchronize()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    shell_ms, geo_ms, launches = dw.kernel_ms()
+    step_ms = [s_.elapsed_time(e_) for s_, e_ in zip(starts, ends)]
+    shell_ms, geo_ms, grp_ms, launches = dw.kernel_ms()
     ctx.set_timing(False)
     t_ms = float(np.sum(step_ms))
     if dist:
@@ -217,6 +217,25 @@ def run_ours(args):
     geo_avg_ms = geo_ms / args.steps
     peak, peak_kind = peaks()
     achieved = ab / (geo_avg_ms / 1e3) / 1e9
+    splat_bytes = int(res["svl_total"].astype(np.int64).sum()) * 2
+    step_bytes = ab + 2 * splat_bytes  # + grouping: splats read and written once more
+    # plain path: one launch per chunk and pass, same world and modes
+    dw.rebuild(LOD_MAX, persistent=False, plain=True)
+    dw.finish()
+    plain_ms = []
+    for _ in range(2):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            a_ = torch.cuda.Event(enable_timing=True)
+            b_ = torch.cuda.Event(enable_timing=True)
+            a_.record(stream)
+        dw.rebuild(LOD_MAX, persistent=False, plain=True)
+        with torch.cuda.stream(stream):
+            b_.record(stream)
+        ctx.sync()
+        torch.cuda.synchronize()
+        plain_ms.append(a_.elapsed_time(b_))
+    plain_value = world.nchunks / (float(np.median(plain_ms)) / 1e3)
     # end to end through the C ABI with host buffers
     e2e_t = []
     h2d = world.pool.nbytes + world.off.nbytes + world.len.nbytes + world.shadow.nbytes + modes.nbytes
@@ -226,7 +245,7 @@ def run_ours(args):
         t0 = time.perf_counter()
         dw.upload(world)
         dw.set_modes(modes)
-        dw.rebuild(LOD_MAX)
+        dw.rebuild(LOD_MAX, group=True)
         dw.finish()
         r = dw.results()
         tot_svl = int(np.max(r["svl_off"] + r["svl_total"])) if len(r) else 0
@@ -253,15 +272,20 @@ def run_ours(args):
         "data": "synthetic (seeded integer-hash terrain + caves; no dataset)",
         "config": workload_config(world, modes),
         "voxels_per_s": round(value * world.R ** 3, 1),
-        "kernel_ms": {"shell": round(shell_ms / args.steps, 4), "geometry": round(geo_avg_ms, 4)},
+        "kernel_ms": {"shell": round(shell_ms / args.steps, 4), "geometry": round(geo_avg_ms, 4),
+                      "group": round(grp_ms / args.steps, 4)},
+        "plain": {"value": round(plain_value, 1), "unit": "chunks/s", "launches_per_step": 2 * world.nchunks,
+                  "batched_over_plain": round(value / plain_value, 2)},
         "e2e": {"value": round(e2e_value, 1), "unit": "chunks/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
-                "path": "vp_world_upload + vp_world_rebuild + vp_world_finish + results/arena readback"},
+                "path": "vp_world_upload + vp_world_rebuild(group) + vp_world_finish + results/arena readback"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None,
                      "kernel": "k_geometry<6>", "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": int(ab),
-                     "bytes_split": {"rle_in": rle_b, "geometry_out": out_b, "shadow_map": sh_b}},
+                     "bytes_split": {"rle_in": rle_b, "geometry_out": out_b, "shadow_map": sh_b},
+                     "step_bytes": int(step_bytes),
+                     "step_frac": round(step_bytes / (t_ms / args.steps / 1e3) / 1e9 / peak, 4)},
         "gpu_launches": int(launches),
     }
     if rank == 0:

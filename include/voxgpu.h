@@ -127,11 +127,12 @@ VP_API int vp_rle_decode(vp_ctx *ctx, const uint32_t *words, uint32_t nwords, ui
 			 uint32_t *out_len);
 
 /* Kernel timing: with timing on, every rebuild records CUDA events around
- * its kernels on the context stream; vp_world_kernel_ms returns the summed
- * milliseconds of the shell pass and the geometry pass since the last call
- * (waits for the stream) and resets them. */
+ * its passes on the context stream; vp_world_kernel_ms waits for the stream
+ * and returns the summed milliseconds since the last call of ms[0] the shell
+ * pass, ms[1] the geometry pass and ms[2] the grouping (n <= 3 values), and
+ * the number of kernel launches, then resets them. */
 VP_API int vp_ctx_set_timing(vp_ctx *ctx, int on);
-VP_API int vp_world_kernel_ms(vp_world *w, double *shell_ms, double *geometry_ms, uint32_t *launches);
+VP_API int vp_world_kernel_ms(vp_world *w, double *ms, int n, uint32_t *launches);
 
 #ifdef __cplusplus
 }

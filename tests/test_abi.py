@@ -4,6 +4,9 @@ import ctypes
 import glob
 import os
 import re
+import subprocess
+
+import pytest
 
 from voxplat_gb300 import build
 
@@ -38,3 +41,24 @@ def test_error_strings_without_gpu():
     lib.vp_strerror.restype = ctypes.c_char_p
     assert lib.vp_strerror(0) == b"ok"
     assert lib.vp_strerror(-4) == b"output overflow"
+
+
+def _probe(tmp_path, name, extra):
+    exe = str(tmp_path / name)
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "abi", "layout_probe.c")
+    subprocess.check_call(["gcc", "-O0", "-o", exe, src] + extra)
+    return subprocess.check_output([exe]).decode()
+
+
+def test_chunkset_layout_matches_reference(tmp_path):
+    ref = os.environ.get("VP_REFERENCE", "/root/reference")
+    if not os.path.exists(os.path.join(ref, "src", "chunkset.h")):
+        pytest.skip("reference sources not present")
+    ours = _probe(tmp_path, "ours", ["-I", INCLUDE])
+    theirs = _probe(tmp_path, "theirs", ["-DUSE_REFERENCE", "-I", os.path.join(ref, "src")])
+    assert ours == theirs
+
+
+def test_dropin_harness_compiles(tmp_path):
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "dropin_harness.c")
+    subprocess.check_call(["gcc", "-O1", "-fsyntax-only", "-I", INCLUDE, src])

@@ -16,94 +16,17 @@
 
 using namespace vp;
 
-namespace {
+#include "vp_internal.h"
 
-thread_local std::string g_cuda_err;
+thread_local std::string vpi_cuda_err;
 
-int cuda_fail(cudaError_t e, const char *what)
+int vpi_cuda_fail(cudaError_t e, const char *what)
 {
 	char buf[256];
 	snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
-	g_cuda_err = buf;
+	vpi_cuda_err = buf;
 	return e == cudaErrorMemoryAllocation ? VP_ENOMEM : VP_ECUDA;
 }
-
-#define CK(call)                                                  \
-	do {                                                      \
-		cudaError_t e_ = (call);                          \
-		if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
-	} while (0)
-
-template <typename T>
-int dev_alloc(T **p, size_t n)
-{
-	*p = nullptr;
-	if (n == 0) n = 1;
-	cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
-	if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
-	return VP_OK;
-}
-
-template <typename T>
-void dev_free(T *&p)
-{
-	if (p) cudaFree((void *)p);
-	p = nullptr;
-}
-
-} // namespace
-
-struct vp_ctx {
-	int device;
-	cudaStream_t stream;
-	int timing;
-	int sm_count;
-	/* staging for the host-buffer codec calls */
-	uint8_t *d_bytes = nullptr;
-	size_t bytes_cap = 0;
-	uint32_t *d_words = nullptr;
-	size_t words_cap = 0;
-	uint64_t *d_scalars = nullptr; /* [0] cursor, [1] off, [2] len|status */
-};
-
-struct vp_world {
-	vp_ctx *ctx;
-	int root_bitw;
-	int max_bitw[3];
-	uint32_t nchunks;
-	uint32_t *d_pool = nullptr;
-	uint64_t pool_words = 0;
-	uint64_t *d_off = nullptr;
-	uint32_t *d_len = nullptr;
-	uint16_t *d_shadow = nullptr;
-	uint64_t shadow_len = 0;
-	uint32_t shadow_w = 0;
-	uint64_t *d_shell_bits = nullptr;
-	uint8_t *d_shell_col = nullptr;
-	SetDesc *d_set = nullptr;
-	WorkItem *d_items = nullptr;
-	std::vector<uint8_t> modes;
-	std::vector<uint32_t> hlen;              /* host copy of stream lengths */
-	bool items_dirty = true;
-	ChunkOut *d_outs = nullptr;
-	unsigned int *d_queue = nullptr;
-	unsigned long long *d_cursors = nullptr; /* svl, vbo, ibo */
-	void *d_arena[3] = {nullptr, nullptr, nullptr};
-	uint64_t cap[3] = {0, 0, 0};             /* 16-byte units */
-	int last_lod = 4;
-	unsigned last_flags = 0;
-	bool uploaded = false;
-	/* grouping */
-	uint64_t *d_gcounts = nullptr, *d_gtotal = nullptr, *d_node_off = nullptr;
-	uint32_t *d_node_items = nullptr;
-	int16_t *d_garena = nullptr;
-	uint64_t garena_units = 0;
-	int grouped_lod = -1;
-	std::vector<cudaEvent_t> ev;             /* pairs per kernel */
-	std::vector<int> ev_kind;                /* 0 shell, 1 geometry */
-	double ms[2] = {0, 0};
-	uint32_t launches = 0;
-};
 
 extern "C" {
 
@@ -122,7 +45,7 @@ VP_API const char *vp_strerror(int code)
 	}
 }
 
-VP_API const char *vp_last_cuda_error(void) { return g_cuda_err.c_str(); }
+VP_API const char *vp_last_cuda_error(void) { return vpi_cuda_err.c_str(); }
 
 VP_API int vp_ctx_create(int device, vp_ctx **out)
 {
@@ -322,7 +245,7 @@ static int validate_stream(const uint32_t *s, uint32_t n, uint64_t N)
 	return sum == N ? VP_OK : VP_EINVAL;
 }
 
-static int upload_setdesc(vp_world *w)
+int vpi_upload_setdesc(vp_world *w)
 {
 	SetDesc d;
 	memset(&d, 0, sizeof(d));
@@ -337,6 +260,8 @@ static int upload_setdesc(vp_world *w)
 	d.nchunks = w->nchunks;
 	d.root_bitw = (uint32_t)w->root_bitw;
 	for (int i = 0; i < 3; i++) d.max_bitw[i] = (uint32_t)w->max_bitw[i];
+	for (int i = 0; i < 3; i++) d.origin[i] = w->origin[i];
+	d.shadow_base = w->shadow_base;
 	CK(cudaMemcpyAsync(w->d_set, &d, sizeof(d), cudaMemcpyHostToDevice, w->ctx->stream));
 	CK(cudaStreamSynchronize(w->ctx->stream));
 	return VP_OK;
@@ -381,7 +306,7 @@ VP_API int vp_world_upload(vp_world *w, const uint32_t *pool, uint64_t pool_word
 	w->shadow_len = shadow_len;
 	w->shadow_w = shadow_w;
 	w->uploaded = true;
-	return upload_setdesc(w);
+	return vpi_upload_setdesc(w);
 }
 
 VP_API int vp_world_set_modes(vp_world *w, const uint8_t *make_mesh)
@@ -420,7 +345,7 @@ static int ensure_items(vp_world *w)
 	return VP_OK;
 }
 
-static int ensure_arenas(vp_world *w)
+int vpi_ensure_arenas(vp_world *w)
 {
 	/* first guess: 64 KiB of each output per chunk, at least 16 MiB */
 	for (int a = 0; a < 3; a++) {
@@ -470,7 +395,7 @@ static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 	vp_ctx *ctx = w->ctx;
 	cudaStream_t st = ctx->stream;
 	int rc;
-	if ((rc = ensure_items(w)) || (rc = ensure_arenas(w))) return rc;
+	if ((rc = ensure_items(w)) || (rc = vpi_ensure_arenas(w))) return rc;
 	CK(cudaMemsetAsync(w->d_cursors, 0, 3 * sizeof(unsigned long long), st));
 	CK(cudaMemsetAsync(w->d_queue, 0, sizeof(unsigned int), st));
 	GeoLaunch L;
@@ -494,11 +419,12 @@ static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 		L.queue = w->d_queue;
 		L.ctas = (uint32_t)(ctx->sm_count * std::max(per_sm, 1));
 	}
-	cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+	cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr, e3 = nullptr;
 	if (ctx->timing) {
 		cudaEventCreate(&e0);
 		cudaEventCreate(&e1);
 		cudaEventCreate(&e2);
+		cudaEventCreate(&e3);
 		cudaEventRecord(e0, st);
 	}
 	cudaError_t e = cudaSuccess;
@@ -537,16 +463,18 @@ static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 		if (e != cudaSuccess) return cuda_fail(e, "geometry launch");
 		w->launches += 2;
 	}
-	if (ctx->timing) {
-		cudaEventRecord(e2, st);
-		w->ev.push_back(e0);
-		w->ev.push_back(e1);
-		w->ev.push_back(e2);
-	}
+	if (ctx->timing) cudaEventRecord(e2, st);
 	w->grouped_lod = -1;
 	if (flags & VP_REBUILD_GROUP) {
 		int rc2 = enqueue_group(w, lod_max);
 		if (rc2) return rc2;
+	}
+	if (ctx->timing) {
+		cudaEventRecord(e3, st);
+		w->ev.push_back(e0);
+		w->ev.push_back(e1);
+		w->ev.push_back(e2);
+		w->ev.push_back(e3);
 	}
 	w->last_lod = lod_max;
 	w->last_flags = flags;
@@ -647,25 +575,183 @@ VP_API int vp_world_read_group(vp_world *w, uint64_t off, uint64_t n, int16_t *d
 	return VP_OK;
 }
 
-VP_API int vp_world_kernel_ms(vp_world *w, double *shell_ms, double *geometry_ms, uint32_t *launches)
+VP_API int vp_world_kernel_ms(vp_world *w, double *ms, int n, uint32_t *launches)
 {
-	if (!w) return VP_EINVAL;
+	if (!w || (n > 0 && !ms)) return VP_EINVAL;
 	CK(cudaStreamSynchronize(w->ctx->stream));
-	for (size_t i = 0; i + 2 < w->ev.size(); i += 3) {
-		float a = 0, b = 0;
-		cudaEventElapsedTime(&a, w->ev[i], w->ev[i + 1]);
-		cudaEventElapsedTime(&b, w->ev[i + 1], w->ev[i + 2]);
-		w->ms[0] += a;
-		w->ms[1] += b;
+	for (size_t i = 0; i + 3 < w->ev.size(); i += 4) {
+		for (int k = 0; k < 3; k++) {
+			float t = 0;
+			cudaEventElapsedTime(&t, w->ev[i + k], w->ev[i + k + 1]);
+			w->ms[k] += t;
+		}
 	}
 	for (cudaEvent_t e : w->ev) cudaEventDestroy(e);
 	w->ev.clear();
-	if (shell_ms) *shell_ms = w->ms[0];
-	if (geometry_ms) *geometry_ms = w->ms[1];
+	for (int k = 0; k < n && k < 3; k++) ms[k] = w->ms[k];
 	if (launches) *launches = w->launches;
-	w->ms[0] = w->ms[1] = 0;
+	w->ms[0] = w->ms[1] = w->ms[2] = 0;
 	w->launches = 0;
 	return VP_OK;
 }
 
 } // extern "C"
+
+/* ------------------------------------------------------------------ */
+/* internal helpers for the drop-in layer                             */
+/* ------------------------------------------------------------------ */
+
+int vpi_world_load(vp_world *w, const VpiChunkSrc *src)
+{
+	const uint32_t N = 1u << (3 * w->root_bitw);
+	cudaStream_t st = w->ctx->stream;
+	std::vector<uint64_t> off(w->nchunks);
+	std::vector<uint32_t> len(w->nchunks);
+	std::vector<uint32_t> byte_chunks;
+	uint64_t total = 0;
+	for (uint32_t c = 0; c < w->nchunks; c++) {
+		if (src[c].bytes) {
+			byte_chunks.push_back(c);
+			continue;
+		}
+		const uint32_t n = src[c].words ? src[c].nwords : 2u;
+		off[c] = total;
+		len[c] = n;
+		total += (n + 3u) & ~3u;
+	}
+	const uint64_t rle_words = total;
+	const uint64_t enc_cap = (uint64_t)byte_chunks.size() * ((uint64_t)N + 8u);
+	total += enc_cap + 8u;
+	std::vector<uint32_t> host(rle_words + 8u, 0u);
+	for (uint32_t c = 0; c < w->nchunks; c++) {
+		if (src[c].bytes) continue;
+		if (src[c].words) {
+			memcpy(&host[off[c]], src[c].words, (size_t)len[c] * sizeof(uint32_t));
+		} else {
+			host[off[c]] = N;
+			host[off[c] + 1] = 0;
+		}
+	}
+	CK(cudaStreamSynchronize(st));
+	dev_free(w->d_pool);
+	int rc;
+	if ((rc = dev_alloc(&w->d_pool, total))) return rc;
+	CK(cudaMemsetAsync(w->d_pool, 0, total * sizeof(uint32_t), st));
+	CK(cudaMemcpyAsync(w->d_pool, host.data(), rle_words * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+	if (!byte_chunks.empty()) {
+		const size_t nb = byte_chunks.size();
+		uint8_t *d_vox = nullptr;
+		uint64_t *d_sc = nullptr, *d_eoff = nullptr;
+		uint32_t *d_elen = nullptr;
+		if ((rc = dev_alloc(&d_vox, nb * (size_t)N + 16u)) || (rc = dev_alloc(&d_sc, 2)) ||
+		    (rc = dev_alloc(&d_eoff, nb)) || (rc = dev_alloc(&d_elen, nb))) {
+			dev_free(d_vox);
+			dev_free(d_sc);
+			dev_free(d_eoff);
+			dev_free(d_elen);
+			return rc;
+		}
+		for (size_t k = 0; k < nb; k++)
+			cudaMemcpyAsync(d_vox + k * N, src[byte_chunks[k]].bytes, N, cudaMemcpyHostToDevice, st);
+		cudaMemsetAsync(d_sc, 0, 2 * sizeof(uint64_t), st);
+		cudaError_t e = launch_rle_encode(d_vox, (uint32_t)nb, N, w->d_pool + rle_words, enc_cap,
+						  (unsigned long long *)d_sc, d_eoff, d_elen, (uint32_t *)(d_sc + 1), st);
+		std::vector<uint64_t> eoff(nb);
+		std::vector<uint32_t> elen(nb);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(eoff.data(), d_eoff, nb * 8u, cudaMemcpyDeviceToHost, st);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(elen.data(), d_elen, nb * 4u, cudaMemcpyDeviceToHost, st);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+		dev_free(d_vox);
+		dev_free(d_sc);
+		dev_free(d_eoff);
+		dev_free(d_elen);
+		if (e != cudaSuccess) return cuda_fail(e, "device encode");
+		for (size_t k = 0; k < nb; k++) {
+			off[byte_chunks[k]] = rle_words + eoff[k];
+			len[byte_chunks[k]] = elen[k];
+		}
+	}
+	CK(cudaMemcpyAsync(w->d_off, off.data(), w->nchunks * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+	CK(cudaMemcpyAsync(w->d_len, len.data(), w->nchunks * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+	w->hlen = len;
+	w->pool_words = total;
+	w->uploaded = true;
+	w->items_dirty = true;
+	CK(cudaStreamSynchronize(st));
+	return VP_OK;
+}
+
+int vpi_world_shadow_window(vp_world *w, const uint16_t *map, uint64_t map_len, uint64_t base, uint64_t n,
+			    uint32_t shadow_w, const int32_t origin[3])
+{
+	if (base > map_len) base = map_len;
+	if (base + n > map_len) n = map_len - base;
+	cudaStream_t st = w->ctx->stream;
+	CK(cudaStreamSynchronize(st));
+	dev_free(w->d_shadow);
+	int rc;
+	if ((rc = dev_alloc(&w->d_shadow, n + 8u))) return rc;
+	if (n && map) CK(cudaMemcpyAsync(w->d_shadow, map + base, n * sizeof(uint16_t), cudaMemcpyHostToDevice, st));
+	w->shadow_len = n;
+	w->shadow_base = base;
+	w->shadow_w = shadow_w;
+	for (int i = 0; i < 3; i++) w->origin[i] = origin[i];
+	return vpi_upload_setdesc(w);
+}
+
+int vpi_world_run(vp_world *w, const WorkItem *items, uint32_t n, int lod_max)
+{
+	cudaStream_t st = w->ctx->stream;
+	int rc;
+	if ((rc = vpi_ensure_arenas(w))) return rc;
+	for (int attempt = 0; attempt < 4; attempt++) {
+		std::vector<WorkItem> all(w->nchunks);
+		for (uint32_t c = 0; c < w->nchunks; c++) all[c] = WorkItem{0, c, 0, c};
+		CK(cudaMemcpyAsync(w->d_items, all.data(), all.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, st));
+		WorkItem *d_run = nullptr;
+		if ((rc = dev_alloc(&d_run, n))) return rc;
+		cudaMemcpyAsync(d_run, items, n * sizeof(WorkItem), cudaMemcpyHostToDevice, st);
+		cudaMemsetAsync(w->d_cursors, 0, 3 * sizeof(unsigned long long), st);
+		GeoLaunch L;
+		memset(&L, 0, sizeof(L));
+		L.sets = w->d_set;
+		L.shell_items = w->d_items;
+		L.n_shell = w->nchunks;
+		L.run_shell = 1;
+		L.threads = 512;
+		L.outs = w->d_outs;
+		L.lod_max = lod_max;
+		Arena *ar[3] = {&L.svl, &L.vbo, &L.ibo};
+		for (int a = 0; a < 3; a++) {
+			ar[a]->base = w->d_arena[a];
+			ar[a]->cap_units = w->cap[a];
+			ar[a]->cursor = w->d_cursors + a;
+		}
+		cudaError_t e = launch_geometry(w->root_bitw, L, st);
+		if (e == cudaSuccess) {
+			GeoLaunch Lg = L;
+			Lg.run_shell = 0;
+			Lg.items = d_run;
+			Lg.n_items = n;
+			e = launch_geometry(w->root_bitw, Lg, st);
+		}
+		unsigned long long cur[3] = {0, 0, 0};
+		if (e == cudaSuccess) e = cudaMemcpyAsync(cur, w->d_cursors, sizeof(cur), cudaMemcpyDeviceToHost, st);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+		dev_free(d_run);
+		if (e != cudaSuccess) return cuda_fail(e, "drop-in launch");
+		bool grow = false;
+		for (int a = 0; a < 3; a++) {
+			if (cur[a] <= w->cap[a]) continue;
+			grow = true;
+			const uint64_t units = cur[a] + cur[a] / 4 + 1024;
+			dev_free(w->d_arena[a]);
+			w->cap[a] = 0;
+			cudaError_t e2 = cudaMalloc(&w->d_arena[a], units * 16u);
+			if (e2 != cudaSuccess) return cuda_fail(e2, "cudaMalloc(arena growth)");
+			w->cap[a] = units;
+		}
+		if (!grow) return VP_OK;
+	}
+	return VP_EOVERFLOW;
+}

@@ -35,10 +35,12 @@ struct SetDesc {
 	uint32_t nchunks;
 	uint32_t root_bitw;
 	uint32_t max_bitw[3];
+	int32_t origin[3];     /* chunk coordinates of this set's chunk 0 in the world */
+	uint64_t shadow_base;  /* world index of shadow[0] (a window of the map) */
 };
 
 /* flags of a work item */
-enum : uint32_t { kItemMesh = 1u };
+enum : uint32_t { kItemMesh = 1u, kItemMaskDense = 2u };
 
 struct WorkItem {
 	uint32_t set;
@@ -184,7 +186,8 @@ __device__ __forceinline__ uint32_t block_scan_array(uint32_t *a, int n, uint32_
  * padded length return 0. */
 __device__ __forceinline__ uint32_t shadow_at(const SetDesc &s, uint32_t idx)
 {
-	return (uint64_t)idx < s.shadow_len ? (uint32_t)__ldg(s.shadow + idx) : 0u;
+	const uint64_t i = (uint64_t)idx - s.shadow_base; /* wraps when idx < base */
+	return i < s.shadow_len ? (uint32_t)__ldg(s.shadow + i) : 0u;
 }
 
 /* shadow_sample (src/chunkset/shadow.h:45-63), uint32 index arithmetic. */

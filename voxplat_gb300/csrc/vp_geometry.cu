@@ -974,6 +974,28 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 	}
 }
 
+/* The L0 mask of chunk_make_mask (src/chunkset/mesher.c:377-456) as a dense
+ * (R+1)^3 byte array: every mask cell gets its colour; other cells keep
+ * what `dst` held (the reference's caller zeroes it). */
+template <int RB>
+__device__ void mask_dense(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m, uint8_t *dst)
+{
+	using G = Geo<RB>;
+	constexpr int R = G::R, S1 = G::S;
+	splat_prepare<RB>(m);
+	for (int i = threadIdx.x; i < S1 * S1; i += blockDim.x) {
+		const int y = i % S1, z = i / S1;
+		uint32_t xr;
+		const uint64_t row = e0_row<RB>(m, y, z, xr);
+		uint8_t *line = dst + ((size_t)z * S1 + y) * S1;
+		for (uint64_t b = row; b; b &= b - 1ull) {
+			const int x = __ffsll((long long)b) - 1;
+			line[x] = (uint8_t)mask_colour<RB>(S, stream, m, x, y, z);
+		}
+		if (xr) line[R] = (uint8_t)mask_colour<RB>(S, stream, m, R, y, z);
+	}
+}
+
 template <int RB>
 __global__ void __launch_bounds__(512, 2) k_geometry(const SetDesc *__restrict__ sets, const WorkItem *__restrict__ items,
 						     uint32_t nitems, unsigned int *queue, ChunkOut *outs, Arena asvl,
@@ -994,15 +1016,16 @@ __global__ void __launch_bounds__(512, 2) k_geometry(const SetDesc *__restrict__
 		const WorkItem wi = items[it];
 		const SetDesc S = sets[wi.set];
 		ChunkOut *out = outs + wi.slot;
-		uint32_t cv[3];
+		uint32_t cv[3], wc[3];
 		chunk_coords(S, wi.chunk, cv);
+		for (int k = 0; k < 3; k++) wc[k] = (uint32_t)(S.origin[k] + (int32_t)cv[k]);
 		const uint32_t N = (uint32_t)R * R * R;
 		const bool mesh = (wi.flags & kItemMesh) != 0;
 		load_neighbours(S, cv, m, N);
 		/* an all-air chunk whose +neighbours are all air has no geometry */
 		const bool empty = m.nbr[nbr_slot(0, 0, 0)] < 0 && m.nbr[nbr_slot(1, 0, 0)] < 0 &&
 				   m.nbr[nbr_slot(0, 1, 0)] < 0 && m.nbr[nbr_slot(0, 0, 1)] < 0;
-		if (empty) {
+		if (empty && !(wi.flags & kItemMaskDense)) {
 			if (threadIdx.x == 0) {
 				out->svl_off = out->vbo_off = out->ibo_off = 0;
 				for (int l = 0; l < kMaxLevels; l++) out->svl_items[l] = 0;
@@ -1015,10 +1038,12 @@ __global__ void __launch_bounds__(512, 2) k_geometry(const SetDesc *__restrict__
 		const uint32_t *stream = S.pool + S.off[wi.chunk];
 		decode_chunk<RB>(stream, S.len[wi.chunk] - 1u, m);
 		load_halo<RB>(S, m);
-		if (mesh)
-			mesh_chunk<RB>(S, stream, m, cv, out, avbo, aibo);
+		if (wi.flags & kItemMaskDense)
+			mask_dense<RB>(S, stream, m, (uint8_t *)asvl.base + (size_t)wi.slot * G::S * G::S * G::S);
+		else if (mesh)
+			mesh_chunk<RB>(S, stream, m, wc, out, avbo, aibo);
 		else
-			splat_chunk<RB>(S, stream, m, cv, lod_max, out, asvl);
+			splat_chunk<RB>(S, stream, m, wc, lod_max, out, asvl);
 		__syncthreads();
 	}
 }

@@ -13,8 +13,8 @@
  * is a bijection onto [0, nchunks): the prefix sum of the level-l item
  * counts in key order gives every segment's destination, and node i's
  * buffer starts at the prefix of its first key. One pass scatters counts
- * into key order, one CTA per level scans them, and a warp per chunk copies
- * its segment with 8-byte vector moves (one splat per lane).
+ * into key order, one CTA per level scans them, and a CTA per chunk copies
+ * its segment with 8-byte vector moves (one splat per thread per step).
  */
 #include "vp_dev.cuh"
 #include "vp_group.h"
@@ -103,14 +103,13 @@ __global__ void __launch_bounds__(1024) k_group_scan(uint32_t n, GroupArgs a)
 	if (threadIdx.x == 0) a.level_total[blockIdx.x] = s_carry;
 }
 
-/* one warp per chunk: copy its level-l segment; the first member of each
- * node also records the node's offset and length */
-__global__ void k_group_copy(const ChunkOut *__restrict__ outs, uint32_t nchunks, GroupArgs a)
+/* one CTA per (chunk, level): copy the chunk's level-l segment, one splat
+ * (8 bytes) per thread per step; the first member of each node also records
+ * the node's offset and length */
+__global__ void __launch_bounds__(256) k_group_copy(const ChunkOut *__restrict__ outs, uint32_t nchunks, GroupArgs a)
 {
-	const uint32_t warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	const int lane = threadIdx.x & 31;
+	const uint32_t c = blockIdx.x;
 	const int l = blockIdx.y;
-	const uint32_t c = warp_global;
 	if (c >= nchunks) return;
 	const GroupGeom g = group_geom(a.max_bitw, l);
 	uint32_t node, rank;
@@ -119,21 +118,20 @@ __global__ void k_group_copy(const ChunkOut *__restrict__ outs, uint32_t nchunks
 	for (int k = 0; k < l; k++) lbase += a.level_total[k];
 	const uint64_t *cnt = a.counts + (size_t)l * nchunks;
 	const uint64_t dst_off = lbase + cnt[key];
-	if (rank == 0 && lane == 0) {
+	if (rank == 0 && threadIdx.x == 0) {
 		const uint32_t mbits = g.eb[0] + g.eb[1] + g.eb[2];
 		const uint32_t next_key = (node + 1u) << mbits;
 		const uint64_t end = next_key < nchunks ? cnt[next_key] : a.level_total[l];
 		a.node_off[(size_t)l * nchunks + node] = dst_off;
 		a.node_items[(size_t)l * nchunks + node] = (uint32_t)(end - cnt[key]);
 	}
-	const ChunkOut o = outs[c];
-	const uint32_t items = o.svl_items[l];
+	const uint32_t items = outs[c].svl_items[l];
 	if (!items) return;
-	uint64_t src_off = o.svl_off;
-	for (int k = 0; k < l; k++) src_off += o.svl_items[k];
+	uint64_t src_off = outs[c].svl_off;
+	for (int k = 0; k < l; k++) src_off += outs[c].svl_items[k];
 	const uint2 *src = (const uint2 *)(a.svl + src_off);
 	uint2 *dst = (uint2 *)(a.out + dst_off);
-	for (uint32_t s = lane; s < items / 4u; s += 32u) dst[s] = src[s];
+	for (uint32_t s = threadIdx.x; s < items / 4u; s += blockDim.x) dst[s] = __ldg(src + s);
 }
 
 cudaError_t launch_group(const ChunkOut *outs, uint32_t nchunks, int lod_max, const GroupArgs &a, cudaStream_t st)
@@ -142,7 +140,7 @@ cudaError_t launch_group(const ChunkOut *outs, uint32_t nchunks, int lod_max, co
 	const int L = lod_max + 1;
 	k_group_scatter<<<dim3((nchunks + 255) / 256, L), 256, 0, st>>>(outs, nchunks, a);
 	k_group_scan<<<L, 1024, 0, st>>>(nchunks, a);
-	k_group_copy<<<dim3((nchunks * 32u + 255u) / 256u, L), 256, 0, st>>>(outs, nchunks, a);
+	k_group_copy<<<dim3(nchunks, L), 256, 0, st>>>(outs, nchunks, a);
 	return cudaGetLastError();
 }
 

@@ -1,0 +1,107 @@
+/* vp_internal.h — host-side state shared by the C-ABI translation units. */
+#pragma once
+#include "voxgpu.h"
+#include "vp_geometry.h"
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+using namespace vp;
+
+int vpi_cuda_fail(cudaError_t e, const char *what);
+
+#define CK(call)                                                     \
+	do {                                                         \
+		cudaError_t e_ = (call);                             \
+		if (e_ != cudaSuccess) return vpi_cuda_fail(e_, #call); \
+	} while (0)
+#define cuda_fail vpi_cuda_fail
+
+template <typename T>
+static inline int dev_alloc(T **p, size_t n)
+{
+	*p = nullptr;
+	if (n == 0) n = 1;
+	cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+	if (e != cudaSuccess) return vpi_cuda_fail(e, "cudaMalloc");
+	return VP_OK;
+}
+
+template <typename T>
+static inline void dev_free(T *&p)
+{
+	if (p) cudaFree((void *)p);
+	p = nullptr;
+}
+
+struct vp_ctx {
+	int device;
+	cudaStream_t stream;
+	int timing;
+	int sm_count;
+	/* staging for the host-buffer codec calls */
+	uint8_t *d_bytes = nullptr;
+	size_t bytes_cap = 0;
+	uint32_t *d_words = nullptr;
+	size_t words_cap = 0;
+	uint64_t *d_scalars = nullptr; /* [0] cursor, [1] off, [2] len|status */
+};
+
+struct vp_world {
+	vp_ctx *ctx;
+	int root_bitw;
+	int max_bitw[3];
+	uint32_t nchunks;
+	uint32_t *d_pool = nullptr;
+	uint64_t pool_words = 0;
+	uint64_t *d_off = nullptr;
+	uint32_t *d_len = nullptr;
+	uint16_t *d_shadow = nullptr;
+	uint64_t shadow_len = 0;
+	uint32_t shadow_w = 0;
+	uint64_t *d_shell_bits = nullptr;
+	uint8_t *d_shell_col = nullptr;
+	SetDesc *d_set = nullptr;
+	WorkItem *d_items = nullptr;
+	std::vector<uint8_t> modes;
+	std::vector<uint32_t> hlen;              /* host copy of stream lengths */
+	bool items_dirty = true;
+	ChunkOut *d_outs = nullptr;
+	unsigned int *d_queue = nullptr;
+	unsigned long long *d_cursors = nullptr; /* svl, vbo, ibo */
+	void *d_arena[3] = {nullptr, nullptr, nullptr};
+	uint64_t cap[3] = {0, 0, 0};             /* 16-byte units */
+	int last_lod = 4;
+	unsigned last_flags = 0;
+	bool uploaded = false;
+	/* grouping */
+	uint64_t *d_gcounts = nullptr, *d_gtotal = nullptr, *d_node_off = nullptr;
+	uint32_t *d_node_items = nullptr;
+	int16_t *d_garena = nullptr;
+	uint64_t garena_units = 0;
+	int grouped_lod = -1;
+	int32_t origin[3] = {0, 0, 0};           /* world chunk coords of chunk 0 */
+	uint64_t shadow_base = 0;                /* world index of d_shadow[0] */
+	std::vector<cudaEvent_t> ev;             /* pairs per kernel */
+	std::vector<int> ev_kind;                /* 0 shell, 1 geometry */
+	double ms[3] = {0, 0, 0};
+	uint32_t launches = 0;
+};
+
+
+/* internal helpers shared with the drop-in layer (vp_api.cu) */
+extern "C" int vpi_upload_setdesc(vp_world *w); /* defined inside the C-ABI block */
+extern "C" int vpi_ensure_arenas(vp_world *w);
+
+/* One chunk's data for vpi_world_load: decoded voxels (R^3 bytes), or an
+ * RLE stream, or neither (all air). */
+struct VpiChunkSrc {
+	const uint8_t *bytes;
+	const uint32_t *words;
+	uint32_t nwords; /* including the 0 terminator */
+};
+int vpi_world_load(vp_world *w, const VpiChunkSrc *src);
+int vpi_world_shadow_window(vp_world *w, const uint16_t *map, uint64_t map_len, uint64_t base, uint64_t n,
+			    uint32_t shadow_w, const int32_t origin[3]);
+int vpi_world_run(vp_world *w, const WorkItem *items, uint32_t n, int lod_max);

@@ -85,8 +85,7 @@ def load(build_if_missing=True):
         "vp_world_read_group": (I, [V, U64, U64, V]),
         "vp_rle_encode": (I, [V, V, U32, V, U32, ctypes.POINTER(U32)]),
         "vp_rle_decode": (I, [V, V, U32, V, U32, ctypes.POINTER(U32)]),
-        "vp_world_kernel_ms": (I, [V, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
-                                   ctypes.POINTER(U32)]),
+        "vp_world_kernel_ms": (I, [V, V, I, ctypes.POINTER(U32)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -233,10 +232,11 @@ class DeviceWorld:
         return out
 
     def kernel_ms(self):
-        a, b, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint32()
-        check(self.lib.vp_world_kernel_ms(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)),
-              "vp_world_kernel_ms")
-        return a.value, b.value, n.value
+        """(shell ms, geometry ms, grouping ms, launches) since the last call."""
+        ms = np.zeros(3, np.float64)
+        n = ctypes.c_uint32()
+        check(self.lib.vp_world_kernel_ms(self.h, _p(ms), 3, ctypes.byref(n)), "vp_world_kernel_ms")
+        return float(ms[0]), float(ms[1]), float(ms[2]), n.value
 
     def chunk_splats(self, res, c):
         r = res[c]
