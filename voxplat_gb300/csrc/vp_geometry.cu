@@ -151,6 +151,7 @@ __device__ void decode_chunk(const uint32_t *__restrict__ s, uint32_t nruns, con
 	 * 32-bit word are combined in registers before one shared atomic */
 	constexpr int K = 8;
 	uint32_t tile_start = 0;
+	uint64_t covered = 0;
 	for (uint32_t base = 0; base < nruns; base += (uint32_t)K * blockDim.x) {
 		const uint32_t k0 = base + (uint32_t)K * threadIdx.x;
 		uint32_t w[K];
@@ -175,7 +176,8 @@ __device__ void decode_chunk(const uint32_t *__restrict__ s, uint32_t nruns, con
 			uint32_t cur = 0xFFFFFFFFu, acc_r = 0, acc_t = 0;
 #pragma unroll
 			for (int j = 0; j < K; j++) {
-				if (k0 + j >= nruns) break;
+				/* runs past R^3 voxels (a malformed stream) are dropped */
+				if (k0 + j >= nruns || pos >= (uint32_t)(R * R * R)) break;
 				const uint32_t p = pos;
 				pos += w[j] & 0xFFFFFFu;
 				const bool solid = (w[j] >> 24) != 0;
@@ -200,7 +202,9 @@ __device__ void decode_chunk(const uint32_t *__restrict__ s, uint32_t nruns, con
 				if (acc_t) atomicOr(occ32 + 2 * hidx<RB>(row & (R - 1), row >> RB) + half, acc_t);
 			}
 		}
+		covered += tot;
 		tile_start += tot;
+		if (covered >= (uint64_t)R * R * R) break; /* the chunk is covered */
 	}
 	__syncthreads();
 	/* prefix XOR of the toggle stream and run-start ranks, rows in scan
