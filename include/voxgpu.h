@@ -126,6 +126,29 @@ VP_API int vp_rle_encode(vp_ctx *ctx, const uint8_t *vox, uint32_t length, uint3
 VP_API int vp_rle_decode(vp_ctx *ctx, const uint32_t *words, uint32_t nwords, uint8_t *out, uint32_t out_cap,
 			 uint32_t *out_len);
 
+/* Geometry rebuild of a small chunk set that allocates no memory; it has
+ * no counterpart in the reference. For callers that cannot allocate device
+ * memory when they need geometry: a render or input thread that must not
+ * stall on cudaMalloc's implicit device synchronisation, or an engine whose
+ * own allocator owns all device memory. Every input and output is a device
+ * pointer the caller provides: the chunks' RLE streams laid out as
+ * vp_world_upload lays them out (each stream 16-byte aligned, at least 8
+ * readable words after the last), their word offsets and lengths, the
+ * shadow map, optional per-chunk mesh flags, three output buffers (splats,
+ * vertices, indices; bytes) and one result record per chunk. The working
+ * data lives in a fixed 4 MiB device array the library holds on every GPU
+ * that loads it (enough for 256 chunks of 64^3 or 1024 of 32^3); larger
+ * sets return VP_EOVERFLOW. The first call on a device looks the array up
+ * (cudaGetSymbolAddress) and should come before any stream capture. Calls
+ * share that array: each call resets it, and calls that overlap on the GPU
+ * race. The work is queued on `stream` (asynchronous); a result whose status
+ * is nonzero means an output buffer was too small for that chunk. */
+VP_API int vp_rebuild_noalloc(int device, void *stream, int root_bitw, const int max_bitw[3], const uint32_t *pool,
+			      const uint64_t *off, const uint32_t *len, const uint16_t *shadow, uint64_t shadow_len,
+			      uint32_t shadow_w, const uint8_t *make_mesh, int lod_max, int16_t *svl, uint64_t svl_bytes,
+			      int16_t *vbo, uint64_t vbo_bytes, uint32_t *ibo, uint64_t ibo_bytes,
+			      vp_chunk_result *results);
+
 /* Kernel timing: with timing on, every rebuild records CUDA events around
  * its passes on the context stream; vp_world_kernel_ms waits for the stream
  * and returns the summed milliseconds since the last call of ms[0] the shell
