@@ -159,6 +159,18 @@ def cpu_baseline(world, modes, budget_s=12.0, threads=None):
             "sample": "%d of the %d chunks (random, seed 1), cold decode, same modes/LOD" % (n, world.nchunks)}
 
 
+def ncu_traffic(name="k_geometry_config2_world.md"):
+    """DRAM bytes per launch of k_geometry from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", name)) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return int(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
 def algorithmic_bytes(world, res):
     """Per rebuild: RLE read + splat/mesh output + shadow map read once."""
     rle = int(world.len.astype(np.int64).sum()) * 4
@@ -280,7 +292,8 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(d2h),
                 "path": "vp_world_upload + vp_world_rebuild(group) + vp_world_finish + results/arena readback"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None,
+                     "frac": round(achieved / peak, 4), "traffic": ncu_traffic(),
+                     "traffic_source": "profiles/k_geometry_config2_world.md (ncu dram__bytes_read+write.sum)",
                      "kernel": "k_geometry<6>", "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": int(ab),
                      "bytes_split": {"rle_in": rle_b, "geometry_out": out_b, "shadow_map": sh_b},
