@@ -105,6 +105,49 @@ VP_API int vp_world_read_svl(vp_world *w, uint64_t off, uint64_t n, int16_t *dst
 VP_API int vp_world_read_vbo(vp_world *w, uint64_t off, uint64_t n, int16_t *dst);
 VP_API int vp_world_read_ibo(vp_world *w, uint64_t off, uint64_t n, uint32_t *dst);
 
+/* Sphere edits (chunkset_edit_sphere, src/chunkset/edit.c:179-244): fill
+ * with `voxel`, or carve when voxel == 0; radius <= 250. Edits apply in
+ * array order, exactly as the reference applies them one after the other:
+ * voxel writes skip y < 2 (edit.c:151), fills update the shadow map in the
+ * reference's loop order (src/chunkset/shadow.h:77-89), carves leave it.
+ * Every chunk of an edit's AABB list (the chunks the reference marks dirty)
+ * is re-encoded and its geometry rebuilt in the mode set by
+ * vp_world_set_modes, with the LOD count of the last rebuild; its result
+ * record then points at the new geometry. */
+typedef struct vp_edit {
+	int32_t x, y, z;    /* centre, world voxels */
+	uint32_t radius;
+	uint8_t voxel;
+	uint8_t pad[7];
+	double arrival_s;   /* vp_world_serve: arrival time from the start */
+} vp_edit;
+
+typedef struct vp_serve_stats {
+	uint32_t batches;
+	uint32_t edits;
+	uint32_t max_batch;
+	uint32_t deferred;  /* times an edit waited for free HBM */
+	uint64_t chunks_remeshed;
+	double busy_s;      /* time with a batch on the GPU */
+	double wall_s;
+} vp_serve_stats;
+
+/* Apply edits[0..n) as one batch and rebuild the dirty chunks (synchronous). */
+VP_API int vp_world_edit(vp_world *w, const vp_edit *edits, uint32_t n);
+/* Read back a chunk's current RLE stream (*n words incl. the terminator;
+ * VP_EOVERFLOW when cap is short) and the shadow map (n elements). */
+VP_API int vp_world_chunk_rle(vp_world *w, uint32_t chunk, uint32_t *dst, uint32_t cap, uint32_t *n);
+VP_API int vp_world_read_shadow(vp_world *w, uint16_t *dst, uint64_t n);
+/* The chunks the last edit batch rebuilt. */
+VP_API int vp_world_dirty(vp_world *w, uint32_t *chunks, uint32_t cap, uint32_t *n);
+/* Replay a timed edit trace (arrival_s ascending) in real time with
+ * continuous batching: edits arriving while a batch runs queue up; the next
+ * batch takes the queued edits in order, up to max_batch, as long as its
+ * working memory fits the free HBM minus hbm_reserve bytes. latency_ms[i] =
+ * completion of edit i's batch - its arrival. */
+VP_API int vp_world_serve(vp_world *w, const vp_edit *edits, uint32_t n, uint32_t max_batch, uint64_t hbm_reserve,
+			  double *latency_ms, vp_serve_stats *stats);
+
 /* LOD/octree draw groups of the last rebuild made with VP_REBUILD_GROUP
  * (gfx_update_svl, src/gfx/vsplat.c:209-331, minus the GL upload): for LOD
  * `lod`, node i (numbered flatten3(node, max_bitw - min(lod, max_bitw)))

@@ -229,6 +229,15 @@ VP_API void vp_world_destroy(vp_world *w)
 	dev_free(w->d_node_off);
 	dev_free(w->d_node_items);
 	dev_free(w->d_garena);
+	dev_free(w->d_vols);
+	dev_free(w->d_edit_chunks);
+	dev_free(w->d_dirty);
+	dev_free(w->d_edit_items);
+	dev_free(w->d_new_off);
+	dev_free(w->d_new_len);
+	dev_free(w->d_edit_sc);
+	if (w->h_pin) cudaFreeHost(w->h_pin);
+	if (w->edit_done) cudaEventDestroy(w->edit_done);
 	for (cudaEvent_t e : w->ev) cudaEventDestroy(e);
 	delete w;
 }
@@ -291,10 +300,14 @@ VP_API int vp_world_upload(vp_world *w, const uint32_t *pool, uint64_t pool_word
 	dev_free(w->d_pool);
 	dev_free(w->d_shadow);
 	int rc;
-	if ((rc = dev_alloc(&w->d_pool, total))) return rc;
+	/* headroom at the tail for streams re-encoded by edits */
+	const uint64_t cap = total + total / 4 + (16u << 20);
+	if ((rc = dev_alloc(&w->d_pool, cap))) return rc;
 	if ((rc = dev_alloc(&w->d_shadow, shadow_len + 8))) return rc;
 	cudaStream_t st = w->ctx->stream;
 	CK(cudaMemcpyAsync(w->d_pool, packed.data(), total * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+	w->pool_cap = cap;
+	w->pool_tail = total;
 	CK(cudaMemcpyAsync(w->d_off, noff.data(), w->nchunks * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
 	CK(cudaMemcpyAsync(w->d_len, len, w->nchunks * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
 	CK(cudaMemsetAsync(w->d_shadow, 0, (shadow_len + 8) * sizeof(uint16_t), st));
@@ -675,6 +688,8 @@ int vpi_world_load(vp_world *w, const VpiChunkSrc *src)
 	CK(cudaMemcpyAsync(w->d_len, len.data(), w->nchunks * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
 	w->hlen = len;
 	w->pool_words = total;
+	w->pool_cap = total;
+	w->pool_tail = total;
 	w->uploaded = true;
 	w->items_dirty = true;
 	CK(cudaStreamSynchronize(st));

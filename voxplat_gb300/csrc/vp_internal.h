@@ -82,6 +82,23 @@ struct vp_world {
 	uint64_t garena_units = 0;
 	int grouped_lod = -1;
 	int32_t origin[3] = {0, 0, 0};           /* world chunk coords of chunk 0 */
+	/* edits: the pool grows at its tail, re-encoded streams are appended */
+	uint64_t pool_cap = 0;                   /* words allocated in d_pool */
+	uint64_t pool_tail = 0;                  /* first free word */
+	uint8_t *d_vols = nullptr;               /* decoded volumes of an edit batch */
+	size_t vols_cap = 0;                     /* chunks */
+	void *d_edit_chunks = nullptr;           /* EditChunk lists of a batch */
+	size_t edit_chunks_cap = 0;
+	uint32_t *d_dirty = nullptr;             /* dirty chunk ids of a batch */
+	WorkItem *d_edit_items = nullptr;
+	uint64_t *d_new_off = nullptr;
+	uint32_t *d_new_len = nullptr;
+	size_t dirty_cap = 0;
+	unsigned long long *d_edit_sc = nullptr; /* [0] encode cursor, [1] status */
+	unsigned long long *h_pin = nullptr;     /* pinned: encode cursor, status, 3 arena cursors */
+	std::vector<int32_t> slot_of;            /* chunk -> volume slot during a batch */
+	std::vector<uint32_t> last_dirty;
+	cudaEvent_t edit_done = nullptr;
 	uint64_t shadow_base = 0;                /* world index of d_shadow[0] */
 	std::vector<cudaEvent_t> ev;             /* pairs per kernel */
 	std::vector<int> ev_kind;                /* 0 shell, 1 geometry */

@@ -40,6 +40,28 @@ RESULT_DTYPE = np.dtype([
     ("vbo_items", np.uint32), ("ibo_items", np.uint32), ("status", np.uint32)])
 assert RESULT_DTYPE.itemsize == ctypes.sizeof(ChunkResult)
 
+EDIT_DTYPE = np.dtype([("x", np.int32), ("y", np.int32), ("z", np.int32), ("radius", np.uint32),
+                       ("voxel", np.uint8), ("pad", np.uint8, (7,)), ("arrival_s", np.float64)])
+assert EDIT_DTYPE.itemsize == 32
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [("batches", ctypes.c_uint32), ("edits", ctypes.c_uint32), ("max_batch", ctypes.c_uint32),
+                ("deferred", ctypes.c_uint32), ("chunks_remeshed", ctypes.c_uint64), ("busy_s", ctypes.c_double),
+                ("wall_s", ctypes.c_double)]
+
+
+def make_edits(rows, arrival=None):
+    """vp_edit array from (x, y, z, radius, voxel) rows."""
+    rows = np.asarray(rows)
+    e = np.zeros(len(rows), EDIT_DTYPE)
+    if len(rows):
+        e["x"], e["y"], e["z"] = rows[:, 0], rows[:, 1], rows[:, 2]
+        e["radius"], e["voxel"] = rows[:, 3], rows[:, 4]
+    if arrival is not None:
+        e["arrival_s"] = arrival
+    return e
+
 _lib = None
 
 
@@ -83,6 +105,11 @@ def load(build_if_missing=True):
         "vp_world_read_ibo": (I, [V, U64, U64, V]),
         "vp_world_group_nodes": (I, [V, I, V, V, U32]),
         "vp_world_read_group": (I, [V, U64, U64, V]),
+        "vp_world_edit": (I, [V, V, U32]),
+        "vp_world_dirty": (I, [V, V, U32, ctypes.POINTER(U32)]),
+        "vp_world_serve": (I, [V, V, U32, U32, U64, V, V]),
+        "vp_world_chunk_rle": (I, [V, U32, V, U32, ctypes.POINTER(U32)]),
+        "vp_world_read_shadow": (I, [V, V, U64]),
         "vp_rle_encode": (I, [V, V, U32, V, U32, ctypes.POINTER(U32)]),
         "vp_rle_decode": (I, [V, V, U32, V, U32, ctypes.POINTER(U32)]),
         "vp_world_kernel_ms": (I, [V, V, I, ctypes.POINTER(U32)]),
@@ -237,6 +264,39 @@ class DeviceWorld:
         n = ctypes.c_uint32()
         check(self.lib.vp_world_kernel_ms(self.h, _p(ms), 3, ctypes.byref(n)), "vp_world_kernel_ms")
         return float(ms[0]), float(ms[1]), float(ms[2]), n.value
+
+    def edit(self, edits):
+        """Apply a batch of edits (EDIT_DTYPE array) and rebuild the dirty chunks."""
+        edits = np.ascontiguousarray(edits, dtype=EDIT_DTYPE)
+        check(self.lib.vp_world_edit(self.h, _p(edits), len(edits)), "vp_world_edit")
+
+    def dirty(self):
+        n = ctypes.c_uint32()
+        check(self.lib.vp_world_dirty(self.h, None, 0, ctypes.byref(n)), "vp_world_dirty")
+        out = np.zeros(n.value, np.uint32)
+        check(self.lib.vp_world_dirty(self.h, _p(out), len(out), ctypes.byref(n)), "vp_world_dirty")
+        return out
+
+    def serve(self, edits, max_batch=64, hbm_reserve=1 << 30):
+        """Replay a timed trace; returns (latency_ms array, ServeStats)."""
+        edits = np.ascontiguousarray(edits, dtype=EDIT_DTYPE)
+        lat = np.zeros(len(edits), np.float64)
+        st = ServeStats()
+        check(self.lib.vp_world_serve(self.h, _p(edits), len(edits), max_batch, hbm_reserve, _p(lat),
+                                      ctypes.byref(st)), "vp_world_serve")
+        return lat, st
+
+    def chunk_rle(self, c):
+        n = ctypes.c_uint32()
+        self.lib.vp_world_chunk_rle(self.h, c, None, 0, ctypes.byref(n))
+        out = np.zeros(n.value, np.uint32)
+        check(self.lib.vp_world_chunk_rle(self.h, c, _p(out), len(out), ctypes.byref(n)), "vp_world_chunk_rle")
+        return out
+
+    def shadow(self, n):
+        out = np.zeros(int(n), np.uint16)
+        check(self.lib.vp_world_read_shadow(self.h, _p(out), int(n)), "vp_world_read_shadow")
+        return out
 
     def chunk_splats(self, res, c):
         r = res[c]
