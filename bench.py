@@ -303,11 +303,79 @@ def run_ours(args):
     }
     if rank == 0:
         out["clocks"] = clk.summary()
+        dw.close()
+        if not args.skip_edits:
+            out["edit_serving"] = edit_serving(ctx)
         out["cpu_baseline"] = cpu_baseline(world, modes)
         print(json.dumps(out), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def edit_trace(seed, n, rate, extent_xz, band=(8, 56), rmax=32):
+    """Poisson arrivals at `rate`/s; spheres with r ~ U[1, rmax], centres
+    uniform over the surface band, half carves and half fills (colour
+    uniform 1..255)."""
+    from voxplat_gb300 import gpu
+    rng = np.random.default_rng(seed)
+    arrival = np.cumsum(rng.exponential(1.0 / rate, n))
+    rows = np.zeros((n, 5), np.int64)
+    rows[:, 0] = rng.integers(0, extent_xz, n)
+    rows[:, 1] = rng.integers(band[0], band[1] + 1, n)
+    rows[:, 2] = rng.integers(0, extent_xz, n)
+    rows[:, 3] = rng.integers(1, rmax + 1, n)
+    fill = rng.random(n) < 0.5
+    rows[:, 4] = np.where(fill, rng.integers(1, 256, n), 0)
+    return gpu.make_edits(rows, arrival)
+
+
+def edit_serving(ctx, seconds=2.0, rate=2000.0, seed=4):
+    """8192x512x8192 world of 64^3 chunks (small terrain, heights 8..56),
+    generated and kept RLE-resident on the device with all geometry; a
+    Poisson trace of sphere edits replayed in real time with continuous
+    batching. Latency = edit arrival -> its chunks re-encoded and remeshed."""
+    import torch
+    from voxplat_gb300 import gpu
+    from voxplat_gb300 import worldgen as wg
+    t0 = time.perf_counter()
+    dw = gpu.DeviceWorld.generated(ctx, wg.TERRAIN_SMALL, 6, (7, 3, 7), seed=7)
+    gen_s = time.perf_counter() - t0
+    n = dw.nchunks
+    c = np.arange(n)
+    xs = (c & 127) * 64 + 32
+    ys = ((c >> 7) & 7) * 64 + 32
+    zs = (c >> 10) * 64 + 32
+    modes = (np.sqrt((xs - 4096.0) ** 2 + (ys - 32.0) ** 2 + (zs - 4096.0) ** 2) < MESH_RADIUS).astype(np.uint8)
+    dw.set_modes(modes)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dw.rebuild(LOD_MAX)
+    dw.finish()
+    rebuild_s = time.perf_counter() - t0
+    edits = edit_trace(seed, int(seconds * rate), rate, 8192)
+    warm = edit_trace(seed + 1, 200, rate, 8192)
+    dw.serve(warm, max_batch=64)
+    lat, st = dw.serve(edits, max_batch=64)
+    out = {
+        "workload": "8192x512x8192 world (128x8x128 chunks of 64^3), small terrain, RLE-resident; "
+                    "Poisson sphere edits at %d/s, r~U[1,32], 50%% carve / 50%% fill, centres in y 8..56" % rate,
+        "edits": int(st.edits),
+        "p50_ms": round(float(np.percentile(lat, 50)), 4),
+        "p99_ms": round(float(np.percentile(lat, 99)), 4),
+        "max_ms": round(float(lat.max()), 4),
+        "batches": int(st.batches),
+        "mean_batch": round(st.edits / max(st.batches, 1), 2),
+        "max_batch": int(st.max_batch),
+        "deferred": int(st.deferred),
+        "chunks_remeshed_per_s": round(st.chunks_remeshed / st.wall_s, 1),
+        "gpu_busy_frac": round(st.busy_s / st.wall_s, 3),
+        "world_gen_s": round(gen_s, 2),
+        "full_rebuild_ms": round(rebuild_s * 1e3, 2),
+        "full_rebuild_chunks_per_s": round(n / rebuild_s, 1),
+    }
+    dw.close()
+    return out
 
 
 def run_reference(args):
@@ -360,6 +428,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-edits", action="store_true", help="skip the edit-serving sub-benchmark")
     args = ap.parse_args()
     import __graft_entry__
     __graft_entry__.build()

@@ -90,6 +90,13 @@ VP_API void vp_world_destroy(vp_world *w);
 VP_API int vp_world_upload(vp_world *w, const uint32_t *pool, uint64_t pool_words, const uint64_t *off,
 			   const uint32_t *len, const uint16_t *shadow, uint64_t shadow_len, uint32_t shadow_w);
 
+/* Generate a seeded synthetic world directly in device memory (RLE pool
+ * and shadow map), bit-identical to the host generator
+ * (voxplat_gb300/csrc/vp_worldgen.h): kind 1 = small terrain (heights
+ * 8..56), kind 2 = terrain + caves (heights 40..200); horizontal noise
+ * scaled by 2^hshift; the shadow map gets pad_rows zero rows. */
+VP_API int vp_world_generate(vp_world *w, int kind, uint64_t seed, int hshift, uint32_t pad_rows);
+
 /* Per chunk: 1 = quad mesh (near chunk, ChunkMD.make_mesh), 0 = splats.
  * NULL = every chunk splats. */
 VP_API int vp_world_set_modes(vp_world *w, const uint8_t *make_mesh);

@@ -6,6 +6,7 @@
 #include "vp_geometry.h"
 #include "vp_rle.h"
 #include "vp_group.h"
+#include "vp_gen.h"
 
 #include <algorithm>
 #include <cstdio>
@@ -319,6 +320,92 @@ VP_API int vp_world_upload(vp_world *w, const uint32_t *pool, uint64_t pool_word
 	w->shadow_len = shadow_len;
 	w->shadow_w = shadow_w;
 	w->uploaded = true;
+	return vpi_upload_setdesc(w);
+}
+
+VP_API int vp_world_generate(vp_world *w, int kind, uint64_t seed, int hshift, uint32_t pad_rows)
+{
+	if (!w || (kind != 1 && kind != 2) || hshift < 0 || hshift > 8) return VP_EINVAL;
+	CK(cudaSetDevice(w->ctx->device));
+	cudaStream_t st = w->ctx->stream;
+	const uint32_t rb = (uint32_t)w->root_bitw, R = 1u << rb, N = R * R * R;
+	const uint32_t nslab = 1u << (w->max_bitw[0] + w->max_bitw[1]);
+	const uint32_t nz = 1u << w->max_bitw[2];
+	GenArgs a;
+	a.kind = (uint32_t)kind;
+	a.seed = seed;
+	a.hshift = hshift;
+	a.root_bitw = rb;
+	for (int i = 0; i < 3; i++) a.max_bitw[i] = (uint32_t)w->max_bitw[i];
+	a.shadow_w = ((1u << w->max_bitw[0]) + (1u << w->max_bitw[1])) * R;
+	const uint64_t Z = (uint64_t)nz * R;
+	CK(cudaStreamSynchronize(st));
+	dev_free(w->d_shadow);
+	dev_free(w->d_pool);
+	int rc;
+	const uint64_t slen = (uint64_t)a.shadow_w * (Z + pad_rows);
+	if ((rc = dev_alloc(&w->d_shadow, slen + 8))) return rc;
+	CK(cudaMemsetAsync(w->d_shadow, 0, (slen + 8) * 2u, st));
+	/* pool: a first guess, grown (with copy) when a slab does not fit */
+	uint64_t cap = (uint64_t)w->nchunks * 2048u + (uint64_t)nslab * (N + 8u) + (1u << 20);
+	if ((rc = dev_alloc(&w->d_pool, cap))) return rc;
+	uint8_t *vols = nullptr;
+	uint64_t *noff = nullptr, *sc = nullptr;
+	uint32_t *nlen = nullptr;
+	if ((rc = dev_alloc(&vols, (size_t)nslab * N + 16u)) || (rc = dev_alloc(&noff, nslab)) ||
+	    (rc = dev_alloc(&nlen, nslab)) || (rc = dev_alloc(&sc, 2))) {
+		dev_free(vols);
+		dev_free(noff);
+		dev_free(nlen);
+		return rc;
+	}
+	uint64_t tail = 0;
+	cudaError_t e = cudaSuccess;
+	for (uint32_t cz = 0; cz < nz && e == cudaSuccess && !rc; cz++) {
+		e = launch_gen_slab(a, cz, vols, st);
+		if (e == cudaSuccess) e = launch_gen_shadow(a, cz, vols, w->d_shadow, slen, st);
+		for (int attempt = 0; attempt < 2 && e == cudaSuccess; attempt++) {
+			unsigned long long h[2] = {0, 0};
+			e = cudaMemsetAsync(sc, 0, 2 * sizeof(uint64_t), st);
+			if (e == cudaSuccess)
+				e = launch_rle_encode(vols, nslab, N, w->d_pool + tail, cap - tail, (unsigned long long *)sc,
+						      noff, nlen, (uint32_t *)(sc + 1), st);
+			if (e == cudaSuccess) e = cudaMemcpyAsync(h, sc, sizeof(h), cudaMemcpyDeviceToHost, st);
+			if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+			if (e != cudaSuccess) break;
+			if (!((uint32_t)h[1] & kStatusOverflow)) {
+				e = launch_scatter_slab(noff, nlen, nslab, cz * nslab, tail, w->d_off, w->d_len, st);
+				tail += h[0];
+				break;
+			}
+			/* grow the pool, keeping what is written */
+			const uint64_t ncap = cap + cap / 2 + (uint64_t)nslab * (N + 8u);
+			uint32_t *np = nullptr;
+			if ((rc = dev_alloc(&np, ncap))) break;
+			e = cudaMemcpyAsync(np, w->d_pool, tail * 4u, cudaMemcpyDeviceToDevice, st);
+			if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+			dev_free(w->d_pool);
+			w->d_pool = np;
+			cap = ncap;
+		}
+	}
+	dev_free(vols);
+	dev_free(noff);
+	dev_free(nlen);
+	dev_free(sc);
+	if (rc) return rc;
+	if (e != cudaSuccess) return cuda_fail(e, "world generation");
+	w->pool_cap = cap;
+	w->pool_tail = tail;
+	w->pool_words = tail;
+	w->shadow_len = slen;
+	w->shadow_w = a.shadow_w;
+	w->shadow_base = 0;
+	w->hlen.resize(w->nchunks);
+	CK(cudaMemcpyAsync(w->hlen.data(), w->d_len, w->nchunks * 4u, cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	w->uploaded = true;
+	w->items_dirty = true;
 	return vpi_upload_setdesc(w);
 }
 

@@ -105,6 +105,7 @@ def load(build_if_missing=True):
         "vp_world_read_ibo": (I, [V, U64, U64, V]),
         "vp_world_group_nodes": (I, [V, I, V, V, U32]),
         "vp_world_read_group": (I, [V, U64, U64, V]),
+        "vp_world_generate": (I, [V, I, U64, I, U32]),
         "vp_world_edit": (I, [V, V, U32]),
         "vp_world_dirty": (I, [V, V, U32, ctypes.POINTER(U32)]),
         "vp_world_serve": (I, [V, V, U32, U32, U64, V, V]),
@@ -184,16 +185,28 @@ class Context:
 class DeviceWorld:
     """A device-resident world (one reference ChunkSet)."""
 
-    def __init__(self, ctx, world):
+    def __init__(self, ctx, world=None, root_bitw=None, max_bitw=None):
         self.ctx = ctx
         self.lib = ctx.lib
         self.world = world
-        self.nchunks = world.nchunks
+        if world is not None:
+            root_bitw, max_bitw = world.root_bitw, world.max_bitw
+        self.root_bitw = root_bitw
+        self.max_bitw = tuple(max_bitw)
+        self.nchunks = 1 << sum(self.max_bitw)
         h = ctypes.c_void_p()
-        mb = (ctypes.c_int * 3)(*world.max_bitw)
-        check(self.lib.vp_world_create(ctx.h, world.root_bitw, mb, ctypes.byref(h)), "vp_world_create")
+        mb = (ctypes.c_int * 3)(*self.max_bitw)
+        check(self.lib.vp_world_create(ctx.h, root_bitw, mb, ctypes.byref(h)), "vp_world_create")
         self.h = h
-        self.upload(world)
+        if world is not None:
+            self.upload(world)
+
+    @classmethod
+    def generated(cls, ctx, kind, root_bitw, max_bitw, seed, hshift=0, pad_rows=66):
+        """A world generated on the device (same bits as worldgen.terrain)."""
+        dw = cls(ctx, None, root_bitw, max_bitw)
+        check(dw.lib.vp_world_generate(dw.h, kind, seed, hshift, pad_rows), "vp_world_generate")
+        return dw
 
     def upload(self, world):
         check(self.lib.vp_world_upload(self.h, _p(world.pool), len(world.pool), _p(world.off), _p(world.len),
