@@ -237,6 +237,9 @@ VP_API void vp_world_destroy(vp_world *w)
 	dev_free(w->d_new_off);
 	dev_free(w->d_new_len);
 	dev_free(w->d_edit_sc);
+	dev_free(w->d_tile_scratch);
+	dev_free(w->d_nruns);
+	dev_free(w->d_run_scratch);
 	if (w->h_pin) cudaFreeHost(w->h_pin);
 	if (w->edit_done) cudaEventDestroy(w->edit_done);
 	for (cudaEvent_t e : w->ev) cudaEventDestroy(e);
@@ -395,6 +398,17 @@ VP_API int vp_world_generate(vp_world *w, int kind, uint64_t seed, int hshift, u
 	dev_free(sc);
 	if (rc) return rc;
 	if (e != cudaSuccess) return cuda_fail(e, "world generation");
+	/* headroom at the tail for streams re-encoded by edits */
+	const uint64_t want = tail + tail / 4 + (64u << 20);
+	if (cap < want) {
+		uint32_t *np = nullptr;
+		if ((rc = dev_alloc(&np, want))) return rc;
+		CK(cudaMemcpyAsync(np, w->d_pool, tail * 4u, cudaMemcpyDeviceToDevice, st));
+		CK(cudaStreamSynchronize(st));
+		dev_free(w->d_pool);
+		w->d_pool = np;
+		cap = want;
+	}
 	w->pool_cap = cap;
 	w->pool_tail = tail;
 	w->pool_words = tail;

@@ -10,9 +10,11 @@
  *   - blocks [nchunks, nchunks + rows): fill edits only, one per world z
  *     row of the AABB. shadow_place_update reads and writes map entries
  *     (x + y) + W*z and its +1 neighbour, always inside row z, so rows are
- *     independent; inside a row the updates are order dependent and run
- *     serially in the reference's order (chunks x-outer then y, then u.x,
- *     then u.y) on a shared-memory copy of the row segment.
+ *     independent; inside a row the updates are order dependent: they run
+ *     in the reference's order (chunks x-outer then y, then u.x, then u.y)
+ *     on a shared-memory copy of the row segment, one column (all u.y of one
+ *     u.x) at a time, which is exact because no update of a column reads an
+ *     entry an earlier update of the same column wrote.
  * The reference's test sqrtf(d0^2 + d1^2 + d2^2) < (float)r equals
  * d0^2 + d1^2 + d2^2 < r^2 for integer d and r < 4096: the squares are exact
  * in float and sqrtf is correctly rounded.
@@ -75,21 +77,32 @@ __global__ void __launch_bounds__(256) k_edit(EditDesc e, const EditChunk *__res
 	}
 	if (threadIdx.x == 0) s_base = (uint32_t)first;
 	__syncthreads();
-	if (threadIdx.x == 0) {
+	/* Updates along one column (fixed chunk and x, y ascending) read
+	 * entries x+y and x+y+1 and write x+y: no step reads an entry an earlier
+	 * step of the same column wrote, so a column is applied at once (warp 0,
+	 * lane per y); columns follow the reference's order. */
+	if (threadIdx.x < 32) {
 		const uint32_t base = s_base;
+		const int lane = threadIdx.x;
 		for (uint32_t k = 0; k < e.nlist; k++) {
 			const EditChunk ch = chunks[k];
 			if (ch.cv[2] * R > z || z >= ch.cv[2] * R + R) continue;
 			const int32_t x0 = max(mn[0], ch.cv[0] * R), x1 = min(mx[0], ch.cv[0] * R + R);
 			const int32_t y0 = max(mn[1], ch.cv[1] * R), y1 = min(mx[1], ch.cv[1] * R + R);
 			for (int32_t x = x0; x < x1; x++)
-				for (int32_t y = y0; y < y1; y++) {
-					if (!in_sphere(x, y, z, e)) continue;
-					/* shadow_sample: shadowed unless both entries < y + 1 */
-					const uint32_t idx = ((uint32_t)x + (uint32_t)y) + shadow_w * (uint32_t)z;
-					const uint32_t j = idx - base;
-					const uint32_t lim = (uint32_t)y + 1u;
-					if (seg[j] < lim && seg[j + 1] < lim) seg[j] = (uint16_t)y;
+				for (int32_t yb = y0; yb < y1; yb += 32) {
+					const int32_t y = yb + lane;
+					bool upd = false;
+					uint32_t j = 0;
+					if (y < y1 && in_sphere(x, y, z, e)) {
+						/* shadow_sample: shadowed unless both entries < y + 1 */
+						j = (((uint32_t)x + (uint32_t)y) + shadow_w * (uint32_t)z) - base;
+						const uint32_t lim = (uint32_t)y + 1u;
+						upd = seg[j] < lim && seg[j + 1] < lim;
+					}
+					__syncwarp();
+					if (upd) seg[j] = (uint16_t)y;
+					__syncwarp();
 				}
 		}
 	}

@@ -12,7 +12,7 @@
  *                  shared memory and shadow_place_update (src/chunkset/
  *                  shadow.h:77-89) runs for every solid voxel of the row in
  *                  the canonical order (chunk index ascending, then x, then
- *                  y ascending), 32 voxels of a column tested per ballot;
+ *                  y ascending), a column of 32 voxels at a time;
  *   the RLE encoder then appends the slab's streams to the world's pool.
  */
 #include "vp_dev.cuh"
@@ -130,8 +130,8 @@ __global__ void __launch_bounds__(256) k_gen_chunk(GenArgs a, uint32_t cz, uint8
 /* Shadow rows of one slab. Candidates in canonical order: chunk index
  * ascending (cy outer, cx inner for a fixed cz), x ascending, y ascending.
  * Each chunk's plane z is staged in shared memory (coalesced), then warp 0
- * walks it: one ballot tests 32 voxels of a column, lane 0 applies the
- * order-dependent updates of the solid ones to the staged map row. */
+ * walks it column by column and applies each column's updates to the
+ * staged map row at once. */
 __global__ void __launch_bounds__(256) k_gen_shadow(GenArgs a, uint32_t cz, const uint8_t *__restrict__ vols,
 						    uint16_t *shadow, uint64_t shadow_len)
 {
@@ -152,23 +152,24 @@ __global__ void __launch_bounds__(256) k_gen_shadow(GenArgs a, uint32_t cz, cons
 				*(uint32_t *)(plane + i) = *(const uint32_t *)(vol + i);
 			__syncthreads();
 			if (threadIdx.x >= 32) continue;
+			/* one column (x) at a time: its updates read entries x+y and
+			 * x+y+1, which no earlier update of the column wrote, so the
+			 * lanes apply the whole column at once */
 			for (int x = 0; x < R; x++)
 				for (int yb = 0; yb < R; yb += 32) {
 					const int y = yb + lane;
-					const bool solid = y < R && plane[x + R * y] != 0;
-					uint32_t m = __ballot_sync(kFull, solid);
-					if (lane == 0) {
-						while (m) {
-							const int yy = yb + __ffs(m) - 1;
-							m &= m - 1;
-							const uint32_t X = (cx << RB) + x, Y = (cy << RB) + yy;
-							const uint32_t j = X + Y; /* index within the row */
-							const uint32_t lim = Y + 1;
-							const uint32_t v0 = row[j];
-							const uint32_t v1 = j + 1 < W ? row[j + 1] : 0u;
-							if (v0 < lim && v1 < lim) row[j] = (uint16_t)Y;
-						}
+					bool upd = false;
+					uint32_t j = 0, Y = 0;
+					if (y < R && plane[x + R * y] != 0) {
+						const uint32_t X = (cx << RB) + x;
+						Y = (cy << RB) + y;
+						j = X + Y; /* index within the row */
+						const uint32_t lim = Y + 1;
+						const uint32_t v1 = j + 1 < W ? row[j + 1] : 0u;
+						upd = row[j] < lim && v1 < lim;
 					}
+					__syncwarp();
+					if (upd) row[j] = (uint16_t)Y;
 					__syncwarp();
 				}
 		}

@@ -95,6 +95,12 @@ struct vp_world {
 	uint32_t *d_new_len = nullptr;
 	size_t dirty_cap = 0;
 	unsigned long long *d_edit_sc = nullptr; /* [0] encode cursor, [1] status */
+	uint32_t *d_tile_scratch = nullptr;      /* tile sums of the tile-parallel codec */
+	size_t tile_cap = 0;
+	uint32_t *d_nruns = nullptr;
+	size_t nruns_cap = 0;
+	uint32_t *d_run_scratch = nullptr;       /* packed run starts while re-encoding */
+	size_t run_scratch_cap = 0;
 	unsigned long long *h_pin = nullptr;     /* pinned: encode cursor, status, 3 arena cursors */
 	std::vector<int32_t> slot_of;            /* chunk -> volume slot during a batch */
 	std::vector<uint32_t> last_dirty;

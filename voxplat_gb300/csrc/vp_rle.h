@@ -18,4 +18,18 @@ cudaError_t launch_rle_decode_bytes(const uint32_t *pool, const uint64_t *off, c
 				    const uint32_t *chunks, uint32_t n, uint32_t N, uint8_t *vox, uint32_t *status,
 				    cudaStream_t st);
 
+/* Tile-parallel variants for a few chunks (many CTAs per chunk).
+ * Decode: tile_scratch holds n * (N/4096 + 2) words. Encode: tile_scratch
+ * n * (N/8192 + 1) words, nruns n words, run_scratch n * (N + 1) words;
+ * the voxel volumes must be padded to 16 bytes. */
+cudaError_t launch_rle_decode_tiles(const uint32_t *pool, const uint64_t *off, const uint32_t *len, const uint32_t *chunks,
+				    uint32_t n, uint32_t N, uint8_t *vox, uint32_t *tile_scratch, cudaStream_t st);
+cudaError_t launch_rle_encode_tiles(const uint8_t *vox, uint32_t n, uint32_t N, uint32_t *pool, uint64_t cap_words,
+				    unsigned long long *cursor, uint64_t *out_off, uint32_t *out_len, uint32_t *status,
+				    uint32_t *tile_scratch, uint32_t *nruns, uint32_t *run_scratch, cudaStream_t st);
+
+/* dst[noff[c] ..] = src[off[c] ..], len[c] words, for every chunk c. */
+cudaError_t launch_copy_streams(const uint32_t *src, const uint64_t *off, const uint32_t *len, const uint64_t *noff,
+				uint32_t *dst, uint32_t nchunks, cudaStream_t st);
+
 } // namespace vp

@@ -4,10 +4,11 @@
  * An edit batch (edits applied in arrival order, src/chunkset/edit.c:
  * 179-244 per edit) runs entirely on the device:
  *   1. every chunk in any edit's AABB list (the reference marks exactly
- *      these dirty, edit.c:241-242) is decoded into a volume;
+ *      these dirty, edit.c:241-242) is decoded into a volume (tile-parallel:
+ *      many CTAs per chunk, so a few long streams still fill the GPU);
  *   2. one k_edit launch per edit, in order (voxels + shadow rows);
- *   3. the volumes are re-encoded (rle_compress) and appended at the pool's
- *      tail, and the chunks' stream offsets are redirected to them;
+ *   3. the volumes are re-encoded (rle_compress, tile-parallel) and appended
+ *      at the pool's tail, and the chunks' stream offsets are redirected;
  *   4. the dirty chunks' shells are rewritten and their geometry rebuilt
  *      (mesh or splats by their mode), appended to the output arenas; the
  *      chunk records point at the new geometry.
@@ -81,13 +82,12 @@ int grow(T **p, size_t &cap, size_t need)
 	return VP_OK;
 }
 
-/* Copy the live streams into a fresh pool with new headroom. */
+/* Copy the live streams into a fresh pool with new headroom (one copy
+ * kernel; the old pool is freed afterwards). */
 int compact_pool(vp_world *w, uint64_t extra_words)
 {
 	cudaStream_t st = w->ctx->stream;
-	std::vector<uint64_t> off(w->nchunks);
 	std::vector<uint32_t> len(w->nchunks);
-	CK(cudaMemcpyAsync(off.data(), w->d_off, w->nchunks * 8u, cudaMemcpyDeviceToHost, st));
 	CK(cudaMemcpyAsync(len.data(), w->d_len, w->nchunks * 4u, cudaMemcpyDeviceToHost, st));
 	CK(cudaStreamSynchronize(st));
 	std::vector<uint64_t> noff(w->nchunks);
@@ -96,15 +96,24 @@ int compact_pool(vp_world *w, uint64_t extra_words)
 		noff[c] = total;
 		total += (len[c] + 3u) & ~3u;
 	}
-	const uint64_t cap = total + total / 4 + extra_words + 8u;
+	const uint64_t cap = total + total / 4 + extra_words + (16u << 20);
 	uint32_t *np = nullptr;
+	uint64_t *d_noff = nullptr;
 	int rc = dev_alloc(&np, cap);
-	if (rc) return rc;
-	CK(cudaMemsetAsync(np, 0, cap * 4u, st));
-	for (uint32_t c = 0; c < w->nchunks; c++)
-		CK(cudaMemcpyAsync(np + noff[c], w->d_pool + off[c], len[c] * 4u, cudaMemcpyDeviceToDevice, st));
-	CK(cudaMemcpyAsync(w->d_off, noff.data(), w->nchunks * 8u, cudaMemcpyHostToDevice, st));
-	CK(cudaStreamSynchronize(st));
+	if (!rc) rc = dev_alloc(&d_noff, w->nchunks);
+	if (rc) {
+		dev_free(np);
+		return rc;
+	}
+	cudaError_t e = cudaMemcpyAsync(d_noff, noff.data(), w->nchunks * 8u, cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess) e = launch_copy_streams(w->d_pool, w->d_off, w->d_len, d_noff, np, w->nchunks, st);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(w->d_off, d_noff, w->nchunks * 8u, cudaMemcpyDeviceToDevice, st);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+	dev_free(d_noff);
+	if (e != cudaSuccess) {
+		dev_free(np);
+		return cuda_fail(e, "pool compaction");
+	}
 	dev_free(w->d_pool);
 	w->d_pool = np;
 	w->pool_cap = cap;
@@ -222,6 +231,15 @@ int enqueue_batch(vp_world *w, const vp_edit *edits, uint32_t n)
 		w->dirty_cap = m;
 	}
 	if (!w->d_edit_sc && (rc = dev_alloc(&w->d_edit_sc, 2))) return rc;
+	{
+		size_t c1 = w->tile_cap, c2 = w->nruns_cap, c3 = w->run_scratch_cap;
+		if ((rc = grow(&w->d_tile_scratch, c1, (size_t)nd * (N / 4096u + 2u)))) return rc;
+		if ((rc = grow(&w->d_nruns, c2, nd))) return rc;
+		if ((rc = grow(&w->d_run_scratch, c3, (size_t)nd * (N + 1u)))) return rc;
+		w->tile_cap = c1;
+		w->nruns_cap = c2;
+		w->run_scratch_cap = c3;
+	}
 	if (!w->h_pin) CK(cudaMallocHost((void **)&w->h_pin, 8 * sizeof(unsigned long long)));
 	if (!w->edit_done) CK(cudaEventCreateWithFlags(&w->edit_done, cudaEventDisableTiming));
 	if ((rc = vpi_ensure_arenas(w))) return rc;
@@ -232,8 +250,8 @@ int enqueue_batch(vp_world *w, const vp_edit *edits, uint32_t n)
 	CK(cudaMemcpyAsync(w->d_edit_items, items.data(), nd * sizeof(WorkItem), cudaMemcpyHostToDevice, st));
 	CK(cudaMemsetAsync(w->d_edit_sc, 0, 2 * sizeof(unsigned long long), st));
 	/* 1. decode */
-	cudaError_t e = launch_rle_decode_bytes(w->d_pool, w->d_off, w->d_len, w->d_dirty, nd, N, w->d_vols,
-						(uint32_t *)(w->d_edit_sc + 1), st);
+	cudaError_t e = launch_rle_decode_tiles(w->d_pool, w->d_off, w->d_len, w->d_dirty, nd, N, w->d_vols,
+						w->d_tile_scratch, st);
 	if (e != cudaSuccess) return cuda_fail(e, "edit decode");
 	/* 2. edits in order */
 	for (uint32_t i = 0; i < n; i++) {
@@ -249,8 +267,9 @@ int enqueue_batch(vp_world *w, const vp_edit *edits, uint32_t n)
 		if (e != cudaSuccess) return cuda_fail(e, "edit launch");
 	}
 	/* 3. re-encode at the pool's tail and redirect the streams */
-	e = launch_rle_encode(w->d_vols, nd, N, w->d_pool + w->pool_tail, w->pool_cap - w->pool_tail, w->d_edit_sc,
-			      w->d_new_off, w->d_new_len, (uint32_t *)(w->d_edit_sc + 1), st);
+	e = launch_rle_encode_tiles(w->d_vols, nd, N, w->d_pool + w->pool_tail, w->pool_cap - w->pool_tail, w->d_edit_sc,
+				    w->d_new_off, w->d_new_len, (uint32_t *)(w->d_edit_sc + 1), w->d_tile_scratch,
+				    w->d_nruns, w->d_run_scratch, st);
 	if (e == cudaSuccess)
 		e = launch_scatter_streams(w->d_dirty, nd, w->d_new_off, w->d_new_len, w->pool_tail, w->d_off, w->d_len,
 					   st);
