@@ -101,6 +101,12 @@ VP_API int vp_world_generate(vp_world *w, int kind, uint64_t seed, int hshift, u
  * NULL = every chunk splats. */
 VP_API int vp_world_set_modes(vp_world *w, const uint8_t *make_mesh);
 
+/* Size the three output arenas (splat lists, vertex and index buffers) to
+ * bytes[0..2], rounded up to 16 B; a caller that knows its output sizes
+ * avoids the grow-and-rerun of vp_world_finish. The default is 16 KiB per
+ * chunk for each arena, at least 16 MiB. Not while a rebuild is in flight. */
+VP_API int vp_world_reserve(vp_world *w, const uint64_t bytes[3]);
+
 /* Enqueue a full rebuild on the context stream (asynchronous). */
 VP_API int vp_world_rebuild(vp_world *w, int lod_max, unsigned flags);
 /* Wait for the rebuild; grow the output arenas and rebuild again if any
@@ -145,6 +151,8 @@ VP_API int vp_world_edit(vp_world *w, const vp_edit *edits, uint32_t n);
  * VP_EOVERFLOW when cap is short) and the shadow map (n elements). */
 VP_API int vp_world_chunk_rle(vp_world *w, uint32_t chunk, uint32_t *dst, uint32_t cap, uint32_t *n);
 VP_API int vp_world_read_shadow(vp_world *w, uint16_t *dst, uint64_t n);
+/* Total words of all chunks' current RLE streams (terminators included). */
+VP_API int vp_world_rle_words(vp_world *w, uint64_t *words);
 /* The chunks the last edit batch rebuilt. */
 VP_API int vp_world_dirty(vp_world *w, uint32_t *chunks, uint32_t cap, uint32_t *n);
 /* Replay a timed edit trace (arrival_s ascending) in real time with

@@ -27,3 +27,4 @@ def test_device_world_equals_host_world(ctx, kind, rb, mb, seed, hshift):
     for c in range(host.nchunks):
         assert np.array_equal(dev.chunk_rle(c), host.chunk_rle(c)), c
     assert np.array_equal(dev.shadow(len(host.shadow)), host.shadow)
+    assert dev.rle_bytes() == int(host.len.astype(np.int64).sum()) * 4

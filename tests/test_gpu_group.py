@@ -64,3 +64,37 @@ def test_plain_path_matches_batched(ctx):
             assert np.array_equal(got[0], ref[c][0]) and np.array_equal(got[1], ref[c][1])
         else:
             assert np.array_equal(got, ref[c])
+
+
+def test_overflowing_arenas_grow_and_rerun(ctx):
+    """Arenas of 16 bytes overflow on the first pass: finish() grows them and
+    reruns the rebuild and the grouping, with the same results as a rebuild
+    that fit at once."""
+    w = worlds.cave_world(4, (2, 3, 2), seed=31)
+    modes = (np.arange(w.nchunks) % 5 == 0).astype(np.uint8)
+    got = []
+    for tiny in (False, True):
+        dw = gpu.DeviceWorld(ctx, w)
+        dw.set_modes(modes)
+        if tiny:
+            dw.reserve(16, 16, 16)
+        dw.rebuild(lod_max=4, group=True)
+        dw.finish()
+        res = dw.results()
+        assert (res["status"] == 0).all()
+        geo = [dw.chunk_mesh(res, c) if modes[c] else dw.chunk_splats(res, c)[0] for c in range(w.nchunks)]
+        groups = []
+        for lod in range(5):
+            off, nit = dw.group_nodes(lod)
+            nodes = 1 << sum(b - min(lod, b) for b in (2, 3, 2))
+            groups.append([dw.read_group(off[i], nit[i]) for i in range(nodes)])
+        got.append((geo, groups))
+        dw.close()
+    (ga, gra), (gb, grb) = got
+    for c in range(w.nchunks):
+        if modes[c]:
+            assert all(np.array_equal(x, y) for x, y in zip(ga[c], gb[c])), c
+        else:
+            assert np.array_equal(ga[c], gb[c]), c
+    for lod in range(5):
+        assert all(np.array_equal(x, y) for x, y in zip(gra[lod], grb[lod])), lod

@@ -461,12 +461,32 @@ static int ensure_items(vp_world *w)
 
 int vpi_ensure_arenas(vp_world *w)
 {
-	/* first guess: 64 KiB of each output per chunk, at least 16 MiB */
+	/* first guess: 16 KiB of each output per chunk, at least 16 MiB; an
+	 * overflowing rebuild grows the arena to what it needed and reruns */
 	for (int a = 0; a < 3; a++) {
 		if (w->d_arena[a]) continue;
-		uint64_t units = std::max<uint64_t>((uint64_t)w->nchunks * 4096u, 1u << 20);
+		uint64_t units = std::max<uint64_t>((uint64_t)w->nchunks * 1024u, 1u << 20);
 		cudaError_t e = cudaMalloc(&w->d_arena[a], units * 16u);
 		if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(arena)");
+		w->cap[a] = units;
+	}
+	return VP_OK;
+}
+
+VP_API int vp_world_reserve(vp_world *w, const uint64_t bytes[3])
+{
+	if (!w || !bytes) return VP_EINVAL;
+	CK(cudaSetDevice(w->ctx->device));
+	CK(cudaStreamSynchronize(w->ctx->stream));
+	for (int a = 0; a < 3; a++) {
+		const uint64_t units = std::max<uint64_t>((bytes[a] + 15u) / 16u, 1u);
+		dev_free(w->d_arena[a]);
+		w->cap[a] = 0;
+		cudaError_t e = cudaMalloc(&w->d_arena[a], units * 16u);
+		if (e != cudaSuccess) {
+			w->d_arena[a] = nullptr;
+			return cuda_fail(e, "cudaMalloc(arena)");
+		}
 		w->cap[a] = units;
 	}
 	return VP_OK;
@@ -497,6 +517,9 @@ static int enqueue_group(vp_world *w, int lod_max)
 	a.node_items = w->d_node_items;
 	a.svl = (const int16_t *)w->d_arena[0];
 	a.out = w->d_garena;
+	a.svl_cursor = w->d_cursors;
+	a.svl_cap_units = w->cap[0];
+	a.out_cap = (uint64_t)w->garena_units * 8u;
 	cudaError_t e = launch_group(w->d_outs, w->nchunks, lod_max, a, st);
 	if (e != cudaSuccess) return cuda_fail(e, "group launch");
 	w->launches += 3;

@@ -15,6 +15,11 @@
  * buffer starts at the prefix of its first key. One pass scatters counts
  * into key order, one CTA per level scans them, and a CTA per chunk copies
  * its segment with 8-byte vector moves (one splat per thread per step).
+ *
+ * A rebuild whose splat arena overflowed left some chunks without lists
+ * (their records carry the overflow status); the copy is then skipped as a
+ * whole, and the host grows the arena and runs the rebuild and the grouping
+ * again.
  */
 #include "vp_dev.cuh"
 #include "vp_group.h"
@@ -111,6 +116,7 @@ __global__ void __launch_bounds__(256) k_group_copy(const ChunkOut *__restrict__
 	const uint32_t c = blockIdx.x;
 	const int l = blockIdx.y;
 	if (c >= nchunks) return;
+	if (*a.svl_cursor > a.svl_cap_units) return; /* overflowed rebuild: rerun follows */
 	const GroupGeom g = group_geom(a.max_bitw, l);
 	uint32_t node, rank;
 	const uint32_t key = group_key(g, c, &node, &rank);
@@ -129,6 +135,7 @@ __global__ void __launch_bounds__(256) k_group_copy(const ChunkOut *__restrict__
 	if (!items) return;
 	uint64_t src_off = outs[c].svl_off;
 	for (int k = 0; k < l; k++) src_off += outs[c].svl_items[k];
+	if (src_off + items > a.svl_cap_units * 8u || dst_off + items > a.out_cap) return;
 	const uint2 *src = (const uint2 *)(a.svl + src_off);
 	uint2 *dst = (uint2 *)(a.out + dst_off);
 	for (uint32_t s = threadIdx.x; s < items / 4u; s += blockDim.x) dst[s] = __ldg(src + s);

@@ -12,6 +12,9 @@ struct GroupArgs {
 	uint32_t *node_items;  /* [levels][nchunks] node length (int16 units) */
 	const int16_t *svl;    /* per-chunk splat lists (the splat arena) */
 	int16_t *out;          /* grouped lists: level 0 nodes, then level 1 ... */
+	const unsigned long long *svl_cursor; /* the splat arena's bump cursor (16 B units) */
+	uint64_t svl_cap_units;               /* the splat arena's capacity (16 B units) */
+	uint64_t out_cap;                     /* capacity of `out` (int16 units) */
 };
 
 cudaError_t launch_group(const ChunkOut *outs, uint32_t nchunks, int lod_max, const GroupArgs &a, cudaStream_t st);

@@ -343,6 +343,18 @@ VP_API int vp_world_chunk_rle(vp_world *w, uint32_t chunk, uint32_t *dst, uint32
 	return VP_OK;
 }
 
+VP_API int vp_world_rle_words(vp_world *w, uint64_t *words)
+{
+	if (!w || !words || !w->uploaded) return VP_EINVAL;
+	std::vector<uint32_t> len(w->nchunks);
+	CK(cudaMemcpyAsync(len.data(), w->d_len, w->nchunks * 4u, cudaMemcpyDeviceToHost, w->ctx->stream));
+	CK(cudaStreamSynchronize(w->ctx->stream));
+	uint64_t t = 0;
+	for (uint32_t l : len) t += l;
+	*words = t;
+	return VP_OK;
+}
+
 VP_API int vp_world_read_shadow(vp_world *w, uint16_t *dst, uint64_t n)
 {
 	if (!w || !dst || n > w->shadow_len) return VP_EINVAL;

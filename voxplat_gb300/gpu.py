@@ -99,6 +99,7 @@ def load(build_if_missing=True):
         "vp_world_set_modes": (I, [V, V]),
         "vp_world_rebuild": (I, [V, I, ctypes.c_uint]),
         "vp_world_finish": (I, [V]),
+        "vp_world_reserve": (I, [V, V]),
         "vp_world_results": (I, [V, V, U32]),
         "vp_world_read_svl": (I, [V, U64, U64, V]),
         "vp_world_read_vbo": (I, [V, U64, U64, V]),
@@ -111,6 +112,7 @@ def load(build_if_missing=True):
         "vp_world_serve": (I, [V, V, U32, U32, U64, V, V]),
         "vp_world_chunk_rle": (I, [V, U32, V, U32, ctypes.POINTER(U32)]),
         "vp_world_read_shadow": (I, [V, V, U64]),
+        "vp_world_rle_words": (I, [V, ctypes.POINTER(U64)]),
         "vp_rle_encode": (I, [V, V, U32, V, U32, ctypes.POINTER(U32)]),
         "vp_rle_decode": (I, [V, V, U32, V, U32, ctypes.POINTER(U32)]),
         "vp_world_kernel_ms": (I, [V, V, I, ctypes.POINTER(U32)]),
@@ -248,6 +250,10 @@ class DeviceWorld:
         check(self.lib.vp_world_read_group(self.h, int(off), int(n), _p(out)), "vp_world_read_group")
         return out
 
+    def reserve(self, svl_bytes, vbo_bytes, ibo_bytes):
+        b = (ctypes.c_uint64 * 3)(svl_bytes, vbo_bytes, ibo_bytes)
+        check(self.lib.vp_world_reserve(self.h, b), "vp_world_reserve")
+
     def finish(self):
         check(self.lib.vp_world_finish(self.h), "vp_world_finish")
 
@@ -305,6 +311,11 @@ class DeviceWorld:
         out = np.zeros(n.value, np.uint32)
         check(self.lib.vp_world_chunk_rle(self.h, c, _p(out), len(out), ctypes.byref(n)), "vp_world_chunk_rle")
         return out
+
+    def rle_bytes(self):
+        n = ctypes.c_uint64()
+        check(self.lib.vp_world_rle_words(self.h, ctypes.byref(n)), "vp_world_rle_words")
+        return n.value * 4
 
     def shadow(self, n):
         out = np.zeros(int(n), np.uint16)
