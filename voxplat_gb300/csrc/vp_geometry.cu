@@ -496,15 +496,54 @@ __device__ void splat_prepare(const Smem &m)
 	}
 }
 
+/* Per chunk size 2^RB and LOD level l: the word offset of the level's rows
+ * in the level-row area, its first 32-row emission group, and the
+ * multiply-shift constant that divides a row index by n = (R >> l) + 1
+ * (q = umulhi(r, magic) equals r / n for every r < 2^17 and n <= 65). */
+struct LevelTab {
+	int off[7][kMaxLevels];
+	int gstart[7][kMaxLevels + 1];
+	uint32_t magic[7][kMaxLevels];
+};
+
+constexpr LevelTab make_level_tab()
+{
+	LevelTab t{};
+	for (int rb = 0; rb < 7; rb++) {
+		const int R = 1 << rb;
+		int off = 0, g = 0;
+		for (int l = 0; l < kMaxLevels; l++) {
+			const int n = (R >> l) + 1;
+			t.off[rb][l] = l == 0 ? 0 : off;
+			if (l >= 1) off += n * n;
+			t.gstart[rb][l] = g;
+			g += (n * n + 31) / 32;
+			t.magic[rb][l] = n == 1 ? 0u : (uint32_t)(0xFFFFFFFFu / (uint32_t)n + 1u);
+		}
+		t.gstart[rb][kMaxLevels] = g;
+	}
+	return t;
+}
+
+__constant__ LevelTab c_lv = make_level_tab();
+
+/* (y, z) of row r of a level with n rows per z and division constant mg */
+__device__ __forceinline__ void row_yz(uint32_t r, uint32_t n, uint32_t mg, int &y, int &z)
+{
+	const uint32_t q = __umulhi(r, mg);
+	z = (int)q;
+	y = (int)(r - q * n);
+}
+
 /* Level-l mask row (y, z); level 0 includes the x = R cell in *xr. */
 template <int RB>
-__device__ __forceinline__ uint64_t level_row(const Smem &m, const int *lvoff, int l, int y, int z, uint32_t &xr)
+__device__ __forceinline__ uint64_t level_row(const Smem &m, int l, int y, int z, uint32_t &xr)
 {
 	constexpr int R = Geo<RB>::R;
 	if (l == 0) return e0_row<RB>(m, y, z, xr);
 	xr = 0;
 	const int n = (R >> l) + 1;
-	return m.lv[lvoff[l] + z * n + y];
+	return m.lv[c_lv.off[RB][l] + z * n + y];
 }
 
 /* Colour of the L0 mask cell (x, y, z) in [0, R]^3: our own voxel, or the
@@ -806,36 +845,32 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
 /* One level-l splat: walk down to the L0 cell whose colour the reference's
  * last-writer-wins downsample keeps (the nonzero child with the largest
  * (z, y, x) at every level, src/chunkset/mesher.c:474-489), then emit
- * {x, y, z, colour | shadow << 6} (src/chunkset/mesher.c:521-531). */
+ * {x, y, z, colour | shadow << 6} (src/chunkset/mesher.c:521-531). At each
+ * level the eight child bits form a pattern indexed dx + 2 dy + 4 dz, and
+ * the chosen child is its highest set bit. */
 template <int RB>
 __device__ __forceinline__ void emit_splat(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m,
-					   const uint32_t cv[3], const int *lvoff, int l, int x, int y, int z, int16_t *dst)
+					   const uint32_t cv[3], int l, int x, int y, int z, int16_t *dst)
 {
 	constexpr int R = Geo<RB>::R;
 	int cx = x, cy = y, cz = z;
-	for (int k2 = l; k2 >= 1; k2--) {
-		const int np = (R >> (k2 - 1)) + 1;
-		uint64_t rows[2][2];
-		uint32_t rx[2][2];
-		for (int dz = 0; dz < 2; dz++)
-			for (int dy = 0; dy < 2; dy++) {
-				const int Y = 2 * cy + dy, Z = 2 * cz + dz;
-				rows[dz][dy] = 0;
-				rx[dz][dy] = 0;
-				if (Y < np && Z < np) rows[dz][dy] = level_row<RB>(m, lvoff, k2 - 1, Y, Z, rx[dz][dy]);
-			}
-		int best = 0;
-		for (int d = 7; d >= 0; d--) {
-			const int dx = d & 1, dy = (d >> 1) & 1, dz = d >> 2;
-			const int X = 2 * cx + dx;
-			if (X >= np) continue;
-			const uint32_t bit = (k2 == 1 && X == R) ? rx[dz][dy] : (uint32_t)((rows[dz][dy] >> X) & 1ull);
-			if (bit) {
-				best = d;
-				break;
+	for (int lc = l - 1; lc >= 0; lc--) {
+		const int np = (R >> lc) + 1;
+		const int X = 2 * cx;
+		uint32_t pat = 0;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			const int Y = 2 * cy + (q & 1), Z = 2 * cz + (q >> 1);
+			if (Y < np && Z < np) {
+				uint32_t xr;
+				const uint64_t row = level_row<RB>(m, lc, Y, Z, xr);
+				/* X is even and R even: X + 1 never equals R */
+				const uint32_t b2 = (lc == 0 && X == R) ? xr : (uint32_t)((row >> X) & 3ull);
+				pat |= b2 << (2 * q);
 			}
 		}
-		cx = 2 * cx + (best & 1);
+		const int best = pat ? 31 - __clz(pat) : 0;
+		cx = X + (best & 1);
 		cy = 2 * cy + ((best >> 1) & 1);
 		cz = 2 * cz + (best >> 2);
 	}
@@ -857,27 +892,16 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 	__shared__ unsigned long long s_base;
 	__shared__ uint32_t s_ok, s_next;
-	int lvoff[kMaxLevels], gfirst[kMaxLevels + 1];
-	{
-		int t = 0;
-		for (int l = 1; l < kMaxLevels; l++) {
-			lvoff[l] = t;
-			t += ((R >> l) + 1) * ((R >> l) + 1);
-		}
-		lvoff[0] = 0;
-		int g = 0;
-		for (int l = 0; l <= kMaxLevels; l++) {
-			gfirst[l] = g;
-			if (l < kMaxLevels && l <= lod_max) g += G::groups_of(((R >> l) + 1) * ((R >> l) + 1));
-		}
-	}
+	const int *gstart = c_lv.gstart[RB];
 	splat_prepare<RB>(m);
 	/* level rows: pairwise OR of the child rows, compacted along x */
 	for (int l = 1; l <= lod_max; l++) {
 		const int n = (R >> l) + 1, np = (R >> (l - 1)) + 1;
-		uint64_t *dst = m.lv + lvoff[l];
+		const uint32_t mg = c_lv.magic[RB][l];
+		uint64_t *dst = m.lv + c_lv.off[RB][l];
 		for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
-			const int y = i % n, z = i / n;
+			int y, z;
+			row_yz((uint32_t)i, (uint32_t)n, mg, y, z);
 			uint64_t acc = 0;
 			uint32_t accx = 0;
 			for (int dz = 0; dz < 2; dz++)
@@ -885,7 +909,7 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 					const int yy = 2 * y + dy, zz = 2 * z + dz;
 					if (yy >= np || zz >= np) continue;
 					uint32_t xr;
-					acc |= level_row<RB>(m, lvoff, l - 1, yy, zz, xr);
+					acc |= level_row<RB>(m, l - 1, yy, zz, xr);
 					accx |= xr;
 				}
 			uint64_t row = compress_pairs(acc);
@@ -895,16 +919,18 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 		__syncthreads();
 	}
 	/* pass 1: splats per 32-row group, levels in order */
-	const int ngroups = gfirst[lod_max + 1];
+	const int ngroups = gstart[lod_max + 1];
 	for (int g = warp; g < ngroups; g += nw) {
 		int l = 0;
-		while (g >= gfirst[l + 1]) l++;
+		while (g >= gstart[l + 1]) l++;
 		const int n = (R >> l) + 1;
-		const int r = (g - gfirst[l]) * 32 + lane;
+		const int r = (g - gstart[l]) * 32 + lane;
 		uint32_t c = 0;
 		if (r < n * n) {
+			int y, z;
+			row_yz((uint32_t)r, (uint32_t)n, c_lv.magic[RB][l], y, z);
 			uint32_t xr;
-			c = __popcll(level_row<RB>(m, lvoff, l, r % n, r / n, xr)) + xr;
+			c = __popcll(level_row<RB>(m, l, y, z, xr)) + xr;
 		}
 #pragma unroll
 		for (int d = 16; d; d >>= 1) c += __shfl_xor_sync(kFull, c, d);
@@ -924,8 +950,8 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 		for (int l = 0; l < kMaxLevels; l++) {
 			uint32_t c = 0;
 			if (l <= lod_max) {
-				const uint32_t b0 = m.grp[gfirst[l]];
-				const uint32_t b1 = gfirst[l + 1] < ngroups ? m.grp[gfirst[l + 1]] : total;
+				const uint32_t b0 = m.grp[gstart[l]];
+				const uint32_t b1 = gstart[l + 1] < ngroups ? m.grp[gstart[l + 1]] : total;
 				c = b1 - b0;
 			}
 			out->svl_items[l] = c * 4u;
@@ -937,42 +963,54 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 	__syncthreads();
 	if (!s_ok) return;
 	int16_t *dst = (int16_t *)asvl.base + s_base * 8u;
-	/* pass 2: warps take groups from a shared counter; one splat per lane */
+	/* pass 2: warps take groups from a shared counter; one splat per lane
+	 * per step, a second one when the group has more than 32 left */
 	for (;;) {
 		uint32_t g = 0;
 		if (lane == 0) g = atomicAdd(&s_next, 1u);
 		g = __shfl_sync(kFull, g, 0);
 		if (g >= (uint32_t)ngroups) break;
 		int l = 0;
-		while ((int)g >= gfirst[l + 1]) l++;
+		while ((int)g >= gstart[l + 1]) l++;
 		const int n = (R >> l) + 1;
-		const int r0 = ((int)g - gfirst[l]) * 32;
-		const int r = r0 + lane;
+		const int r = ((int)g - gstart[l]) * 32 + lane;
 		uint64_t row = 0;
-		uint32_t xr = 0;
-		if (r < n * n) row = level_row<RB>(m, lvoff, l, r % n, r / n, xr);
+		uint32_t xr = 0, yz = 0;
+		if (r < n * n) {
+			int y, z;
+			row_yz((uint32_t)r, (uint32_t)n, c_lv.magic[RB][l], y, z);
+			row = level_row<RB>(m, l, y, z, xr);
+			yz = (uint32_t)y | ((uint32_t)z << 16);
+		}
 		const uint32_t c = __popcll(row) + xr;
 		const uint32_t inc = warp_incl_add(c);
 		const uint32_t excl = inc - c;
 		const uint32_t T = __shfl_sync(kFull, inc, 31);
 		const uint32_t base = m.grp[g];
-		/* two items per lane per step keep twice the loads in flight */
 		for (uint32_t k = 0; k < T; k += 64) {
-			const uint32_t j0 = k + lane, j1 = k + 32 + lane;
-			const int s0 = search_lane(excl, j0), s1 = search_lane(excl, j1);
-			const uint32_t e0 = __shfl_sync(kFull, excl, s0), e1 = __shfl_sync(kFull, excl, s1);
-			const uint64_t w0 = shfl64(row, s0), w1 = shfl64(row, s1);
-			if (j0 < T) {
-				const int k0 = (int)(j0 - e0);
-				const int x0 = k0 < __popcll(w0) ? select_bit(w0, k0) : R;
-				const int r0_ = r0 + s0;
-				emit_splat<RB>(S, stream, m, cv, lvoff, l, x0, r0_ % n, r0_ / n, dst + (size_t)(base + j0) * 4);
+			{
+				const uint32_t j = k + lane;
+				const int s = search_lane(excl, j);
+				const uint32_t e = __shfl_sync(kFull, excl, s), q = __shfl_sync(kFull, yz, s);
+				const uint64_t w = shfl64(row, s);
+				if (j < T) {
+					const int kk = (int)(j - e);
+					const int x = kk < __popcll(w) ? select_bit(w, kk) : R;
+					emit_splat<RB>(S, stream, m, cv, l, x, (int)(q & 0xFFFFu), (int)(q >> 16),
+						       dst + (size_t)(base + j) * 4);
+				}
 			}
-			if (j1 < T) {
-				const int k1 = (int)(j1 - e1);
-				const int x1 = k1 < __popcll(w1) ? select_bit(w1, k1) : R;
-				const int r1_ = r0 + s1;
-				emit_splat<RB>(S, stream, m, cv, lvoff, l, x1, r1_ % n, r1_ / n, dst + (size_t)(base + j1) * 4);
+			if (k + 32 < T) {
+				const uint32_t j = k + 32 + lane;
+				const int s = search_lane(excl, j);
+				const uint32_t e = __shfl_sync(kFull, excl, s), q = __shfl_sync(kFull, yz, s);
+				const uint64_t w = shfl64(row, s);
+				if (j < T) {
+					const int kk = (int)(j - e);
+					const int x = kk < __popcll(w) ? select_bit(w, kk) : R;
+					emit_splat<RB>(S, stream, m, cv, l, x, (int)(q & 0xFFFFu), (int)(q >> 16),
+						       dst + (size_t)(base + j) * 4);
+				}
 			}
 		}
 	}
