@@ -79,6 +79,12 @@ def main():
     for k in picked:
         w = wg.uneven_chunk(3, k)
         save("uneven_k%d" % k, **world_arrays(w), **geometry(ob.RefWorld(w), 1, (4,)))
+    # one sparse standalone 128^3 chunk (the large-chunk path)
+    for k in range(64):
+        if wg.uneven_root_bitw(3, k) == 7 and wg.uneven_occupancy_ppm(3, k) < 3000:
+            w = wg.uneven_chunk(3, k)
+            save("uneven128_k%d" % k, **world_arrays(w), **geometry(ob.RefWorld(w), 1, (4,)))
+            break
     # RLE codec on edge-case voxel arrays
     rng = np.random.default_rng(11)
     cases = {

@@ -41,14 +41,31 @@ def test_cave_world_mixed_modes(ctx, root_bitw, max_bitw):
 
 @pytest.mark.parametrize("k", range(12))
 def test_uneven_chunks(ctx, k):
-    rb = wg.uneven_root_bitw(5, k)
-    if rb > 6:
-        pytest.skip("128^3 chunks take the large-chunk path")
     w = wg.uneven_chunk(5, k)
     o = OracleWorld(w)
     dw = gpu.DeviceWorld(ctx, w)
     assert worlds.compare_world(dw, o, None, 4) == []
     assert worlds.compare_world(dw, o, np.ones(1, np.uint8), 4) == []
+
+
+@pytest.mark.parametrize("max_bitw", [(1, 0, 1), (0, 1, 0)])
+def test_big_chunk_worlds(ctx, max_bitw):
+    """128^3 chunks (two-word rows, working set in global scratch) with
+    neighbours across x and z, or across y."""
+    w = worlds.cave_world(7, max_bitw, seed=21)
+    o = OracleWorld(w)
+    dw = gpu.DeviceWorld(ctx, w)
+    modes = (np.arange(w.nchunks) % 2).astype(np.uint8)
+    assert worlds.compare_world(dw, o, modes, 4) == []
+    assert worlds.compare_world(dw, o, 1 - modes, 5) == []
+
+
+@pytest.mark.parametrize("lod_max", [0, 1, 5, 7])
+def test_big_chunk_lod_levels(ctx, lod_max):
+    w = wg.uneven_chunk(5, 8)
+    assert w.root_bitw == 7
+    dw = gpu.DeviceWorld(ctx, w)
+    assert worlds.compare_world(dw, OracleWorld(w), None, lod_max) == []
 
 
 @pytest.mark.parametrize("lod_max", [0, 1, 5, 7])

@@ -204,6 +204,14 @@ VP_API int vp_world_create(vp_ctx *ctx, int root_bitw, const int max_bitw[3], vp
 		vp_world_destroy(w);
 		return rc;
 	}
+	if (root_bitw == 7) {
+		/* one working set per SM: the 128^3 kernels run one CTA per SM */
+		w->big_slots = (uint32_t)ctx->sm_count;
+		if ((rc = dev_alloc(&w->d_big, (size_t)w->big_slots * big_scratch_slot_bytes()))) {
+			vp_world_destroy(w);
+			return rc;
+		}
+	}
 	*out = w;
 	return VP_OK;
 }
@@ -219,6 +227,7 @@ VP_API void vp_world_destroy(vp_world *w)
 	dev_free(w->d_shadow);
 	dev_free(w->d_shell_bits);
 	dev_free(w->d_shell_col);
+	dev_free(w->d_big);
 	dev_free(w->d_set);
 	dev_free(w->d_items);
 	dev_free(w->d_outs);
@@ -537,6 +546,8 @@ static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 	CK(cudaMemsetAsync(w->d_queue, 0, sizeof(unsigned int), st));
 	GeoLaunch L;
 	memset(&L, 0, sizeof(L));
+	L.big_scratch = w->d_big;
+	L.big_slots = w->big_slots;
 	L.sets = w->d_set;
 	L.items = w->d_items;
 	L.n_items = w->nchunks;
@@ -853,6 +864,8 @@ int vpi_world_run(vp_world *w, const WorkItem *items, uint32_t n, int lod_max)
 		cudaMemsetAsync(w->d_cursors, 0, 3 * sizeof(unsigned long long), st);
 		GeoLaunch L;
 		memset(&L, 0, sizeof(L));
+		L.big_scratch = w->d_big;
+		L.big_slots = w->big_slots;
 		L.sets = w->d_set;
 		L.shell_items = w->d_items;
 		L.n_shell = w->nchunks;

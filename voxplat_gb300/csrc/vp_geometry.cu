@@ -25,6 +25,8 @@
  *   Output space comes from bump-allocated arenas; counts are known before
  *   emission, so every chunk's output is contiguous and in reference order.
  */
+#include <algorithm>
+
 #include "vp_dev.cuh"
 #include "vp_geometry.h"
 
@@ -333,14 +335,14 @@ __device__ __forceinline__ int nbr_slot(int dx, int dy, int dz) { return (dx + 1
 
 /* Fill the 27-entry neighbour table: chunk index, or -1 where the neighbour
  * is outside the world or all air (its shell was not written). */
-__device__ __forceinline__ void load_neighbours(const SetDesc &S, const uint32_t cv[3], const Smem &m, uint32_t N)
+__device__ __forceinline__ void load_neighbours(const SetDesc &S, const uint32_t cv[3], int32_t *nbr, uint32_t N)
 {
 	if (threadIdx.x < 27) {
 		const int t = threadIdx.x;
 		const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
 		int64_t nc = neighbour(S, cv, dx, dy, dz);
 		if (nc >= 0 && chunk_is_null(S, (uint32_t)nc, N)) nc = -1;
-		m.nbr[t] = (int32_t)nc;
+		nbr[t] = (int32_t)nc;
 	}
 	__syncthreads();
 }
@@ -499,17 +501,17 @@ __device__ void splat_prepare(const Smem &m)
 /* Per chunk size 2^RB and LOD level l: the word offset of the level's rows
  * in the level-row area, its first 32-row emission group, and the
  * multiply-shift constant that divides a row index by n = (R >> l) + 1
- * (q = umulhi(r, magic) equals r / n for every r < 2^17 and n <= 65). */
+ * (q = umulhi(r, magic) equals r / n for every r < 2^17 and n <= 129). */
 struct LevelTab {
-	int off[7][kMaxLevels];
-	int gstart[7][kMaxLevels + 1];
-	uint32_t magic[7][kMaxLevels];
+	int off[8][kMaxLevels];
+	int gstart[8][kMaxLevels + 1];
+	uint32_t magic[8][kMaxLevels];
 };
 
 constexpr LevelTab make_level_tab()
 {
 	LevelTab t{};
-	for (int rb = 0; rb < 7; rb++) {
+	for (int rb = 0; rb < 8; rb++) {
 		const int R = 1 << rb;
 		int off = 0, g = 0;
 		for (int l = 0; l < kMaxLevels; l++) {
@@ -616,72 +618,110 @@ __device__ __forceinline__ uint64_t shfl64(uint64_t v, int src)
 	return ((uint64_t)hi << 32) | lo;
 }
 
-/* Quad vertex offsets per visible face axis (lutv, src/chunkset/mesher.c:19-33)
- * and the index pattern (luti, src/chunkset/mesher.c:53-66). */
-__constant__ uint8_t c_quad_offset[3][4][3] = {
-	{{1, 0, 0}, {1, 0, 1}, {1, 1, 1}, {1, 1, 0}},
-	{{0, 1, 0}, {1, 1, 0}, {1, 1, 1}, {0, 1, 1}},
-	{{1, 0, 1}, {0, 0, 1}, {0, 1, 1}, {1, 1, 1}},
+/* Quad vertex offsets per visible face axis (lutv, src/chunkset/mesher.c:
+ * 19-33) packed three bits (x, y, z) per vertex, four vertices per axis:
+ *   axis 0: (1,0,0) (1,0,1) (1,1,1) (1,1,0)
+ *   axis 1: (0,1,0) (1,1,0) (1,1,1) (0,1,1)
+ *   axis 2: (1,0,1) (0,0,1) (0,1,1) (1,1,1)
+ * and the index pattern (luti, src/chunkset/mesher.c:53-66) packed two bits
+ * per index, one six-index sequence per (normal, rotate):
+ *   0,3,1,2,1,3 | 3,2,0,1,0,2 | 1,3,0,3,1,2 | 0,2,3,2,0,1
+ * Held in registers, so lanes with different axes never serialise on a
+ * constant-memory lookup. */
+__device__ __forceinline__ uint32_t quad_offsets(int i)
+{
+	constexpr uint32_t a0 = 1u | (5u << 3) | (7u << 6) | (3u << 9);
+	constexpr uint32_t a1 = 2u | (3u << 3) | (7u << 6) | (6u << 9);
+	constexpr uint32_t a2 = 5u | (4u << 3) | (6u << 6) | (7u << 9);
+	return i == 0 ? a0 : (i == 1 ? a1 : a2);
+}
+
+__device__ __forceinline__ uint32_t quad_indices(int normal, int rotate)
+{
+	constexpr uint32_t q0 = 0u | (3u << 2) | (1u << 4) | (2u << 6) | (1u << 8) | (3u << 10);
+	constexpr uint32_t q1 = 3u | (2u << 2) | (0u << 4) | (1u << 6) | (0u << 8) | (2u << 10);
+	constexpr uint32_t q2 = 1u | (3u << 2) | (0u << 4) | (3u << 6) | (1u << 8) | (2u << 10);
+	constexpr uint32_t q3 = 0u | (2u << 2) | (3u << 4) | (2u << 6) | (0u << 8) | (1u << 10);
+	return normal ? (rotate ? q3 : q2) : (rotate ? q1 : q0);
+}
+
+/* Voxel access of one decoded chunk for the mesher: occupancy anywhere in
+ * [-1, R]^3, the colour of a solid voxel of the chunk, and the colour of an
+ * L0 mask cell (own voxel, or the +neighbour's at coordinate R). */
+template <int RB>
+struct SmallAcc {
+	const SetDesc &S;
+	const uint32_t *__restrict__ stream;
+	const Smem &m;
+	__device__ __forceinline__ uint32_t occ(int x, int y, int z) const { return occ_at<RB>(m, x, y, z); }
+	__device__ __forceinline__ uint32_t colour(int x, int y, int z) const { return colour_at<RB>(stream, m, x, y, z); }
+	__device__ __forceinline__ uint32_t mcolour(int x, int y, int z) const
+	{
+		return mask_colour<RB>(S, stream, m, x, y, z);
+	}
 };
-__constant__ uint8_t c_quad_index[24] = {0, 3, 1, 2, 1, 3, 3, 2, 0, 1, 0, 2,
-					 1, 3, 0, 3, 1, 2, 0, 2, 3, 2, 0, 1};
 
 /* One face: AO from the 8 samples around the air voxel, shadow / diamond
  * from the shadow map, 4 vertices and 6 indices (src/chunkset/mesher.c:
- * 236-349). */
-template <int RB>
-__device__ void emit_face(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m, const uint32_t cv[3],
-			  int x, int y, int z, int i, uint32_t ordinal, int16_t *vbo, uint32_t *ibo)
+ * 236-349). Voxel A = (x, y, z), B = A + e_i; AIR is the air one, BLK the
+ * solid one. */
+template <int RB, class Acc>
+__device__ __forceinline__ void emit_face(const Acc &A, const SetDesc &S, const uint32_t cv[3], int x, int y, int z,
+					  int i, uint32_t ordinal, int16_t *vbo, uint32_t *ibo)
 {
-	const int AC[3] = {x, y, z};
-	int NB[3] = {x, y, z};
-	NB[i] += 1;
-	const uint32_t a_solid = occ_at<RB>(m, x, y, z);
-	const uint32_t colour = a_solid ? colour_at<RB>(stream, m, x, y, z) : mask_colour<RB>(S, stream, m, NB[0], NB[1], NB[2]);
+	const int nx = x + (i == 0), ny = y + (i == 1), nz = z + (i == 2);
+	const uint32_t a_solid = A.occ(x, y, z);
+	const uint32_t colour = a_solid ? A.colour(x, y, z) : A.mcolour(nx, ny, nz);
 	const int normal = a_solid ? 0 : 1;
-	const int *AIR = a_solid ? NB : AC;
-	const int *BLK = a_solid ? AC : NB;
-	const int u = (i == 0) ? 1 : 0;
-	const int v = (i == 2) ? 1 : 2;
-	int O[3];
-#define OCC3(dU, dV) (O[0] = AIR[0], O[1] = AIR[1], O[2] = AIR[2], O[u] += (dU), O[v] += (dV), \
-		      occ_at<RB>(m, O[0], O[1], O[2]))
+	const int ax = a_solid ? nx : x, ay = a_solid ? ny : y, az = a_solid ? nz : z;
+	const int bx = a_solid ? x : nx, by = a_solid ? y : ny, bz = a_solid ? z : nz;
+	/* the two axes other than i: u = y for i = 0 else x; v = y for i = 2
+	 * else z */
+	const int ux = i != 0, uy = i == 0, vy = i == 2, vz = i != 2;
+#define OCC3(dU, dV) A.occ(ax + (dU) * ux, ay + (dU) * uy + (dV) * vy, az + (dV) * vz)
 	const uint32_t an0 = OCC3(-1, 0), an2 = OCC3(1, 0), an1 = OCC3(0, -1), an3 = OCC3(0, 1);
 	const uint32_t ac0 = OCC3(-1, -1), ac1 = OCC3(1, -1), ac2 = OCC3(1, 1), ac3 = OCC3(-1, 1);
 #undef OCC3
 	const uint32_t e0 = (an0 + an1) | ac0, e1 = (an1 + an2) | ac1;
 	const uint32_t e2 = (an2 + an3) | ac2, e3 = (an3 + an0) | ac3;
-	uint32_t va[4];
+	uint32_t va0, va1, va2, va3;
 	if (i == 0) {
-		va[0] = e0; va[3] = e1; va[2] = e2; va[1] = e3;
+		va0 = e0; va3 = e1; va2 = e2; va1 = e3;
 	} else if (i == 1) {
-		va[0] = e0; va[1] = e1; va[2] = e2; va[3] = e3;
+		va0 = e0; va1 = e1; va2 = e2; va3 = e3;
 	} else {
-		va[1] = e0; va[0] = e1; va[3] = e2; va[2] = e3;
+		va1 = e0; va0 = e1; va3 = e2; va2 = e3;
 	}
-	const int rotate = (va[0] + va[2] < va[1] + va[3]) ? 6 : 0;
-	uint32_t ws[3];
-	for (int k = 0; k < 3; k++) ws[k] = (cv[k] << RB) + (uint32_t)BLK[k];
+	const int rotate = (va0 + va2 < va1 + va3) ? 1 : 0;
+	uint32_t wsx = (cv[0] << RB) + (uint32_t)bx;
+	uint32_t wsy = (cv[1] << RB) + (uint32_t)by;
+	uint32_t wsz = (cv[2] << RB) + (uint32_t)bz;
 	uint32_t shadow = 0;
 	if (i == 0 && normal)
-		shadow = shadow_sample_normal(S, ws[0], ws[1], ws[2]);
+		shadow = shadow_sample_normal(S, wsx, wsy, wsz);
 	else if (i == 1 && !normal)
-		shadow = shadow_sample(S, ws[0], ws[1], ws[2]);
-	ws[i] -= (uint32_t)normal;
+		shadow = shadow_sample(S, wsx, wsy, wsz);
+	if (i == 0) wsx -= (uint32_t)normal;
+	else if (i == 1) wsy -= (uint32_t)normal;
+	else wsz -= (uint32_t)normal;
 	uint32_t diamond = 3;
 	if (i == 2) {
 		shadow = 0;
-		const uint32_t sz = ws[2] + (a_solid ? 1u : 0u); /* +1 when B is air */
-		diamond = (uint32_t)(!shadow_sample(S, ws[0], ws[1], sz)) << 1;
-		diamond |= (uint32_t)(!shadow_sample(S, ws[0], ws[1] - 1u, sz));
+		const uint32_t sz = wsz + (a_solid ? 1u : 0u); /* +1 when B is air */
+		diamond = (uint32_t)(!shadow_sample(S, wsx, wsy, sz)) << 1;
+		diamond |= (uint32_t)(!shadow_sample(S, wsx, wsy - 1u, sz));
 	}
+	const uint32_t qo = quad_offsets(i);
+	const uint32_t word0 = colour | ((uint32_t)(i + 3 * normal) << 8) | (shadow << 13) | (diamond << 14);
 	uint32_t out[8];
+	const uint32_t va[4] = {va0, va1, va2, va3};
+#pragma unroll
 	for (int vert = 0; vert < 4; vert++) {
-		const uint32_t px = (ws[0] + c_quad_offset[i][vert][0]) & 0xFFFFu;
-		const uint32_t py = (ws[1] + c_quad_offset[i][vert][1]) & 0xFFFFu;
-		const uint32_t pz = (ws[2] + c_quad_offset[i][vert][2]) & 0xFFFFu;
-		const uint32_t word = (colour | (va[vert] << 6) | ((uint32_t)(i + 3 * normal) << 8) |
-				       ((uint32_t)vert << 11) | (shadow << 13) | (diamond << 14)) & 0xFFFFu;
+		const uint32_t o = qo >> (3 * vert);
+		const uint32_t px = (wsx + (o & 1u)) & 0xFFFFu;
+		const uint32_t py = (wsy + ((o >> 1) & 1u)) & 0xFFFFu;
+		const uint32_t pz = (wsz + ((o >> 2) & 1u)) & 0xFFFFu;
+		const uint32_t word = (word0 | (va[vert] << 6) | ((uint32_t)vert << 11)) & 0xFFFFu;
 		out[2 * vert] = px | (py << 16);
 		out[2 * vert + 1] = pz | (word << 16);
 	}
@@ -689,11 +729,11 @@ __device__ void emit_face(const SetDesc &S, const uint32_t *__restrict__ stream,
 	vd[0] = make_uint4(out[0], out[1], out[2], out[3]);
 	vd[1] = make_uint4(out[4], out[5], out[6], out[7]);
 	const uint32_t vb = ordinal * 4u;
-	const uint8_t *qi = c_quad_index + normal * 12 + rotate;
+	const uint32_t qi = quad_indices(normal, rotate);
 	uint2 *id = (uint2 *)(ibo + (size_t)ordinal * 6);
-	id[0] = make_uint2(vb + qi[0], vb + qi[1]);
-	id[1] = make_uint2(vb + qi[2], vb + qi[3]);
-	id[2] = make_uint2(vb + qi[4], vb + qi[5]);
+	id[0] = make_uint2(vb + (qi & 3u), vb + ((qi >> 2) & 3u));
+	id[1] = make_uint2(vb + ((qi >> 4) & 3u), vb + ((qi >> 6) & 3u));
+	id[2] = make_uint2(vb + ((qi >> 8) & 3u), vb + ((qi >> 10) & 3u));
 }
 
 /* Face bits of row (y, z): bit x of f[i] = face between (x,y,z) and its
@@ -805,6 +845,7 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
 	if (!s_ok || faces == 0) return;
 	int16_t *vbo = (int16_t *)avbo.base + s_base[0] * 8u;
 	uint32_t *ibo = (uint32_t *)aibo.base + s_base[1] * 4u;
+	const SmallAcc<RB> acc{S, stream, m};
 	/* pass 2: warps take 32-row groups from a shared counter; one face per
 	 * lane per step */
 	for (;;) {
@@ -830,13 +871,13 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
 				int x, i;
 				select_face<RB>(ax, ay, az, j0 - e0, x, i);
 				const int rr = (int)g * 32 + s0;
-				emit_face<RB>(S, stream, m, cv, x, rr & (R - 1), rr >> RB, i, base + j0, vbo, ibo);
+				emit_face<RB>(acc, S, cv, x, rr & (R - 1), rr >> RB, i, base + j0, vbo, ibo);
 			}
 			if (j1 < T) {
 				int x, i;
 				select_face<RB>(bx, by, bz, j1 - e1, x, i);
 				const int rr = (int)g * 32 + s1;
-				emit_face<RB>(S, stream, m, cv, x, rr & (R - 1), rr >> RB, i, base + j1, vbo, ibo);
+				emit_face<RB>(acc, S, cv, x, rr & (R - 1), rr >> RB, i, base + j1, vbo, ibo);
 			}
 		}
 	}
@@ -1038,13 +1079,50 @@ __device__ void mask_dense(const SetDesc &S, const uint32_t *__restrict__ stream
 	}
 }
 
+/* One work item of a <= 64^3 chunk: neighbours, decode, halo, then mask /
+ * mesh / splats. Returns with the block synchronised. */
+template <int RB>
+__device__ __forceinline__ void geometry_item(const SetDesc &S, const WorkItem &wi, ChunkOut *out, const Smem &m,
+					      const Arena &asvl, const Arena &avbo, const Arena &aibo, int lod_max)
+{
+	using G = Geo<RB>;
+	constexpr int R = G::R;
+	uint32_t cv[3], wc[3];
+	chunk_coords(S, wi.chunk, cv);
+	for (int k = 0; k < 3; k++) wc[k] = (uint32_t)(S.origin[k] + (int32_t)cv[k]);
+	const uint32_t N = (uint32_t)R * R * R;
+	const bool mesh = (wi.flags & kItemMesh) != 0;
+	load_neighbours(S, cv, m.nbr, N);
+	/* an all-air chunk whose +neighbours are all air has no geometry */
+	const bool empty = m.nbr[nbr_slot(0, 0, 0)] < 0 && m.nbr[nbr_slot(1, 0, 0)] < 0 &&
+			   m.nbr[nbr_slot(0, 1, 0)] < 0 && m.nbr[nbr_slot(0, 0, 1)] < 0;
+	if (empty && !(wi.flags & kItemMaskDense)) {
+		if (threadIdx.x == 0) {
+			out->svl_off = out->vbo_off = out->ibo_off = 0;
+			for (int l = 0; l < kMaxLevels; l++) out->svl_items[l] = 0;
+			out->svl_total = out->vbo_items = out->ibo_items = 0;
+			out->status = 0;
+		}
+		__syncthreads();
+		return;
+	}
+	const uint32_t *stream = S.pool + S.off[wi.chunk];
+	decode_chunk<RB>(stream, S.len[wi.chunk] - 1u, m);
+	load_halo<RB>(S, m);
+	if (wi.flags & kItemMaskDense)
+		mask_dense<RB>(S, stream, m, (uint8_t *)asvl.base + (size_t)wi.slot * G::S * G::S * G::S);
+	else if (mesh)
+		mesh_chunk<RB>(S, stream, m, wc, out, avbo, aibo);
+	else
+		splat_chunk<RB>(S, stream, m, wc, lod_max, out, asvl);
+	__syncthreads();
+}
+
 template <int RB>
 __global__ void __launch_bounds__(512, 2) k_geometry(const SetDesc *__restrict__ sets, const WorkItem *__restrict__ items,
 						     uint32_t nitems, unsigned int *queue, ChunkOut *outs, Arena asvl,
 						     Arena avbo, Arena aibo, int lod_max)
 {
-	using G = Geo<RB>;
-	constexpr int R = G::R;
 	extern __shared__ __align__(16) uint8_t smem[];
 	const Smem m = carve<RB>(smem);
 	__shared__ uint32_t s_item;
@@ -1056,36 +1134,55 @@ __global__ void __launch_bounds__(512, 2) k_geometry(const SetDesc *__restrict__
 		if (it >= nitems) break;
 		next = nitems;
 		const WorkItem wi = items[it];
+		geometry_item<RB>(sets[wi.set], wi, outs + wi.slot, m, asvl, avbo, aibo, lod_max);
+	}
+}
+
+} // namespace vp
+
+#include "vp_geometry_big.cuh"
+
+namespace vp {
+
+/* 128^3 chunks: persistent CTAs, each with its own scratch slot; items come
+ * from the queue, or by a grid stride when there is none. */
+__global__ void __launch_bounds__(512, 1) k_shell_big(const SetDesc *__restrict__ sets, const WorkItem *__restrict__ items,
+						      uint32_t nitems, uint8_t *scratch)
+{
+	__shared__ uint32_t tmp[64];
+	__shared__ int32_t nbr[28];
+	const BigMem m = big_carve(scratch, blockIdx.x, tmp, nbr);
+	const uint32_t N = (uint32_t)Big::R * Big::R * Big::R;
+	for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+		const WorkItem wi = items[it];
 		const SetDesc S = sets[wi.set];
-		ChunkOut *out = outs + wi.slot;
-		uint32_t cv[3], wc[3];
-		chunk_coords(S, wi.chunk, cv);
-		for (int k = 0; k < 3; k++) wc[k] = (uint32_t)(S.origin[k] + (int32_t)cv[k]);
-		const uint32_t N = (uint32_t)R * R * R;
-		const bool mesh = (wi.flags & kItemMesh) != 0;
-		load_neighbours(S, cv, m, N);
-		/* an all-air chunk whose +neighbours are all air has no geometry */
-		const bool empty = m.nbr[nbr_slot(0, 0, 0)] < 0 && m.nbr[nbr_slot(1, 0, 0)] < 0 &&
-				   m.nbr[nbr_slot(0, 1, 0)] < 0 && m.nbr[nbr_slot(0, 0, 1)] < 0;
-		if (empty && !(wi.flags & kItemMaskDense)) {
-			if (threadIdx.x == 0) {
-				out->svl_off = out->vbo_off = out->ibo_off = 0;
-				for (int l = 0; l < kMaxLevels; l++) out->svl_items[l] = 0;
-				out->svl_total = out->vbo_items = out->ibo_items = 0;
-				out->status = 0;
-			}
-			__syncthreads();
-			continue;
-		}
+		if (chunk_is_null(S, wi.chunk, N)) continue;
 		const uint32_t *stream = S.pool + S.off[wi.chunk];
-		decode_chunk<RB>(stream, S.len[wi.chunk] - 1u, m);
-		load_halo<RB>(S, m);
-		if (wi.flags & kItemMaskDense)
-			mask_dense<RB>(S, stream, m, (uint8_t *)asvl.base + (size_t)wi.slot * G::S * G::S * G::S);
-		else if (mesh)
-			mesh_chunk<RB>(S, stream, m, wc, out, avbo, aibo);
-		else
-			splat_chunk<RB>(S, stream, m, wc, lod_max, out, asvl);
+		decode_big(stream, S.len[wi.chunk] - 1u, m);
+		shell_big(stream, m, S.shell_bits + (size_t)wi.chunk * Big::shell_words,
+			  S.shell_col + (size_t)wi.chunk * Big::shell_cols);
+		__syncthreads();
+	}
+}
+
+__global__ void __launch_bounds__(512, 1) k_geometry_big(const SetDesc *__restrict__ sets,
+							 const WorkItem *__restrict__ items, uint32_t nitems,
+							 unsigned int *queue, ChunkOut *outs, Arena asvl, Arena avbo,
+							 Arena aibo, int lod_max, uint8_t *scratch)
+{
+	__shared__ uint32_t tmp[64];
+	__shared__ int32_t nbr[28];
+	__shared__ uint32_t s_item;
+	const BigMem m = big_carve(scratch, blockIdx.x, tmp, nbr);
+	uint32_t next = blockIdx.x;
+	for (;;) {
+		if (threadIdx.x == 0) s_item = queue ? atomicAdd(queue, 1u) : next;
+		__syncthreads();
+		const uint32_t it = s_item;
+		if (it >= nitems) break;
+		next += gridDim.x;
+		const WorkItem wi = items[it];
+		geometry_item_big(sets[wi.set], wi, outs + wi.slot, m, asvl, avbo, aibo, lod_max);
 		__syncthreads();
 	}
 }
@@ -1117,6 +1214,29 @@ static cudaError_t launch_rb(const GeoLaunch &L, cudaStream_t st)
 	return e;
 }
 
+/* 128^3 chunks: shells and geometry by persistent CTAs, one scratch slot
+ * each (grid = min(items, slots)). */
+static cudaError_t launch_big(const GeoLaunch &L, cudaStream_t st)
+{
+	if (!L.big_scratch || !L.big_slots) return cudaErrorInvalidValue;
+	cudaError_t e = cudaSuccess;
+	if (L.run_shell && L.n_shell) {
+		const uint32_t grid = std::min(L.n_shell, L.big_slots);
+		k_shell_big<<<grid, 512, 0, st>>>(L.sets, L.shell_items, L.n_shell, L.big_scratch);
+		e = cudaGetLastError();
+		if (e != cudaSuccess) return e;
+	}
+	if (L.n_items) {
+		const uint32_t grid = std::min(L.n_items, L.big_slots);
+		k_geometry_big<<<grid, 512, 0, st>>>(L.sets, L.items, L.n_items, L.queue, L.outs, L.svl, L.vbo, L.ibo,
+						    L.lod_max, L.big_scratch);
+		e = cudaGetLastError();
+	}
+	return e;
+}
+
+size_t big_scratch_slot_bytes() { return Big::slot_bytes; }
+
 size_t geometry_smem_bytes(int root_bitw)
 {
 	switch (root_bitw) {
@@ -1124,6 +1244,7 @@ size_t geometry_smem_bytes(int root_bitw)
 	case 4: return Geo<4>::bytes;
 	case 5: return Geo<5>::bytes;
 	case 6: return Geo<6>::bytes;
+	case 7: return 1; /* working set in global scratch */
 	default: return 0;
 	}
 }
@@ -1149,7 +1270,10 @@ int geometry_ctas_per_sm(int root_bitw, int threads)
 	}
 }
 
-size_t shell_words_per_chunk(int root_bitw) { return 6u * (1u << root_bitw); }
+size_t shell_words_per_chunk(int root_bitw)
+{
+	return root_bitw == 7 ? Big::shell_words : 6u * (1u << root_bitw);
+}
 size_t shell_cols_per_chunk(int root_bitw) { return 3u * (1u << root_bitw) * (1u << root_bitw); }
 
 cudaError_t launch_geometry(int root_bitw, const GeoLaunch &L, cudaStream_t st)
@@ -1159,6 +1283,7 @@ cudaError_t launch_geometry(int root_bitw, const GeoLaunch &L, cudaStream_t st)
 	case 4: return launch_rb<4>(L, st);
 	case 5: return launch_rb<5>(L, st);
 	case 6: return launch_rb<6>(L, st);
+	case 7: return launch_big(L, st);
 	default: return cudaErrorInvalidValue;
 	}
 }

@@ -17,9 +17,12 @@ struct GeoLaunch {
 	ChunkOut *outs;
 	Arena svl, vbo, ibo;
 	int lod_max;
+	uint8_t *big_scratch;       /* 128^3 chunks: per-CTA working sets */
+	uint32_t big_slots;         /* slots in big_scratch = CTAs of a launch */
 };
 
 size_t geometry_smem_bytes(int root_bitw);
+size_t big_scratch_slot_bytes();
 size_t shell_words_per_chunk(int root_bitw);
 size_t shell_cols_per_chunk(int root_bitw);
 int geometry_ctas_per_sm(int root_bitw, int threads);

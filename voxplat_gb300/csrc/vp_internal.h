@@ -62,6 +62,8 @@ struct vp_world {
 	uint32_t shadow_w = 0;
 	uint64_t *d_shell_bits = nullptr;
 	uint8_t *d_shell_col = nullptr;
+	uint8_t *d_big = nullptr;                /* 128^3 chunks: per-CTA working sets */
+	uint32_t big_slots = 0;
 	SetDesc *d_set = nullptr;
 	WorkItem *d_items = nullptr;
 	std::vector<uint8_t> modes;

@@ -151,6 +151,8 @@ int enqueue_remesh(vp_world *w, uint32_t ndirty)
 	cudaStream_t st = w->ctx->stream;
 	GeoLaunch L;
 	memset(&L, 0, sizeof(L));
+	L.big_scratch = w->d_big;
+	L.big_slots = w->big_slots;
 	L.sets = w->d_set;
 	L.threads = 512;
 	L.outs = w->d_outs;
