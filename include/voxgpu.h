@@ -68,6 +68,7 @@ typedef struct vp_chunk_result {
 #define VP_REBUILD_PERSISTENT 1u /* persistent CTAs + device work queue */
 #define VP_REBUILD_PLAIN 2u      /* one launch per chunk and pass (comparison path) */
 #define VP_REBUILD_GROUP 4u      /* also build the LOD/octree draw groups */
+#define VP_REBUILD_GRAPH 8u      /* batches: replay the tuned configuration's CUDA graph */
 
 VP_API const char *vp_strerror(int code);
 VP_API const char *vp_last_cuda_error(void);
@@ -214,6 +215,50 @@ VP_API int vp_rebuild_noalloc(int device, void *stream, int root_bitw, const int
  * the number of kernel launches, then resets them. */
 VP_API int vp_ctx_set_timing(vp_ctx *ctx, int on);
 VP_API int vp_world_kernel_ms(vp_world *w, double *ms, int n, uint32_t *launches);
+
+/* Batches of standalone chunks of mixed root sizes (8..128): each chunk is
+ * its own 1x1x1 ChunkSet (neighbours are the air null chunk) with its own
+ * shadow map, 2R wide. This is how chunkset_manage (src/chunkset.c:233-507)
+ * meshes chunks of unrelated sets, batched into one GPU pass. */
+typedef struct vp_batch vp_batch;
+
+#define VP_BATCH_MIXED 0 /* one persistent launch over items of every root size */
+#define VP_BATCH_SPLIT 1 /* one persistent launch per root size, run concurrently */
+
+typedef struct vp_batch_tune {
+	int strategy;   /* VP_BATCH_MIXED or VP_BATCH_SPLIT */
+	int min_blocks; /* MIXED: 2 = registers capped for two CTAs per SM, 1 = uncapped */
+	int order;      /* 0 = longest stream first, 1 = by root size then longest (SPLIT needs 1) */
+	uint32_t ctas;  /* MIXED: persistent CTAs, 0 = as many as fit */
+	float ms;       /* vp_batch_autotune: measured rebuild time of this configuration */
+} vp_batch_tune;
+
+VP_API int vp_batch_create(vp_ctx *ctx, uint32_t n, const int *root_bitw, vp_batch **out);
+VP_API void vp_batch_destroy(vp_batch *b);
+/* Streams in the reference format, chunk k at pool[off[k] .. off[k]+len[k]),
+ * and chunk k's shadow map at shadow[shadow_off[k] ..] (shadow_len[k]
+ * entries, padded rows included). */
+VP_API int vp_batch_upload(vp_batch *b, const uint32_t *pool, uint64_t pool_words, const uint64_t *off,
+			   const uint32_t *len, const uint16_t *shadow, const uint64_t *shadow_off,
+			   const uint64_t *shadow_len);
+VP_API int vp_batch_set_modes(vp_batch *b, const uint8_t *make_mesh);
+/* flags: VP_REBUILD_PLAIN = one launch per chunk; VP_REBUILD_GRAPH = replay
+ * the CUDA graph of the tuned configuration (captured on first use and after
+ * arena growth); otherwise the tuned configuration launched directly. */
+VP_API int vp_batch_rebuild(vp_batch *b, int lod_max, unsigned flags);
+VP_API int vp_batch_finish(vp_batch *b);
+/* Time every candidate configuration on this batch (graph replays), keep
+ * the fastest; `tried` (capacity *ntried) receives each with its time. */
+VP_API int vp_batch_autotune(vp_batch *b, int lod_max, vp_batch_tune *best, vp_batch_tune *tried, int *ntried);
+VP_API int vp_batch_set_tune(vp_batch *b, const vp_batch_tune *t);
+VP_API int vp_batch_get_tune(vp_batch *b, vp_batch_tune *t);
+VP_API int vp_batch_results(vp_batch *b, vp_chunk_result *out, uint32_t n);
+VP_API int vp_batch_read_svl(vp_batch *b, uint64_t off, uint64_t n, int16_t *dst);
+VP_API int vp_batch_read_vbo(vp_batch *b, uint64_t off, uint64_t n, int16_t *dst);
+VP_API int vp_batch_read_ibo(vp_batch *b, uint64_t off, uint64_t n, uint32_t *dst);
+/* Summed rebuild time (events around each rebuild while timing is on) and
+ * kernel launches since the last call. */
+VP_API int vp_batch_kernel_ms(vp_batch *b, double *ms, uint32_t *launches);
 
 #ifdef __cplusplus
 }

@@ -255,7 +255,7 @@ VP_API void vp_world_destroy(vp_world *w)
 	delete w;
 }
 
-static int validate_stream(const uint32_t *s, uint32_t n, uint64_t N)
+int vpi_validate_stream(const uint32_t *s, uint32_t n, uint64_t N)
 {
 	if (n < 2 || s[n - 1] != 0) return VP_EINVAL;
 	uint64_t sum = 0;
@@ -299,7 +299,7 @@ VP_API int vp_world_upload(vp_world *w, const uint32_t *pool, uint64_t pool_word
 	uint64_t total = 0;
 	for (uint32_t c = 0; c < w->nchunks; c++) {
 		if (off[c] + len[c] > pool_words) return VP_EINVAL;
-		int rc = validate_stream(pool + off[c], len[c], N);
+		int rc = vpi_validate_stream(pool + off[c], len[c], N);
 		if (rc) return rc;
 		noff[c] = total;
 		total += (len[c] + 3u) & ~3u;

@@ -1134,7 +1134,8 @@ __global__ void __launch_bounds__(512, 2) k_geometry(const SetDesc *__restrict__
 		if (it >= nitems) break;
 		next = nitems;
 		const WorkItem wi = items[it];
-		geometry_item<RB>(sets[wi.set], wi, outs + wi.slot, m, asvl, avbo, aibo, lod_max);
+		const SetDesc S = sets[wi.set];
+		geometry_item<RB>(S, wi, outs + wi.slot, m, asvl, avbo, aibo, lod_max);
 	}
 }
 
@@ -1182,8 +1183,45 @@ __global__ void __launch_bounds__(512, 1) k_geometry_big(const SetDesc *__restri
 		if (it >= nitems) break;
 		next += gridDim.x;
 		const WorkItem wi = items[it];
-		geometry_item_big(sets[wi.set], wi, outs + wi.slot, m, asvl, avbo, aibo, lod_max);
+		const SetDesc S = sets[wi.set];
+		geometry_item_big(S, wi, outs + wi.slot, m, asvl, avbo, aibo, lod_max);
 		__syncthreads();
+	}
+}
+
+/* Work items of any root size 8..128 in one persistent launch: each item
+ * takes the path of its set's root size (the shared-memory carve of its size,
+ * or this CTA's scratch slot for 128^3). Shared memory is sized for 64^3. */
+template <int MINB>
+__global__ void __launch_bounds__(512, MINB) k_geometry_mixed(const SetDesc *__restrict__ sets,
+							      const WorkItem *__restrict__ items, uint32_t nitems,
+							      unsigned int *queue, ChunkOut *outs, Arena asvl,
+							      Arena avbo, Arena aibo, int lod_max, uint8_t *scratch)
+{
+	extern __shared__ __align__(16) uint8_t smem[];
+	__shared__ uint32_t s_item;
+	uint32_t next = blockIdx.x;
+	for (;;) {
+		if (threadIdx.x == 0) s_item = queue ? atomicAdd(queue, 1u) : next;
+		__syncthreads();
+		const uint32_t it = s_item;
+		if (it >= nitems) break;
+		next += gridDim.x;
+		const WorkItem wi = items[it];
+		const SetDesc S = sets[wi.set];
+		ChunkOut *out = outs + wi.slot;
+		switch (S.root_bitw) {
+		case 3: geometry_item<3>(S, wi, out, carve<3>(smem), asvl, avbo, aibo, lod_max); break;
+		case 4: geometry_item<4>(S, wi, out, carve<4>(smem), asvl, avbo, aibo, lod_max); break;
+		case 5: geometry_item<5>(S, wi, out, carve<5>(smem), asvl, avbo, aibo, lod_max); break;
+		case 6: geometry_item<6>(S, wi, out, carve<6>(smem), asvl, avbo, aibo, lod_max); break;
+		default: {
+			const Smem m6 = carve<6>(smem);
+			const BigMem bm = big_carve(scratch, blockIdx.x, m6.tmp, m6.nbr);
+			geometry_item_big(S, wi, out, bm, asvl, avbo, aibo, lod_max);
+			__syncthreads();
+		}
+		}
 	}
 }
 
@@ -1236,6 +1274,46 @@ static cudaError_t launch_big(const GeoLaunch &L, cudaStream_t st)
 }
 
 size_t big_scratch_slot_bytes() { return Big::slot_bytes; }
+
+template <int MINB>
+static int mixed_ctas_per_sm(int threads)
+{
+	int n = 0;
+	cudaFuncSetAttribute(k_geometry_mixed<MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Geo<6>::bytes);
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_geometry_mixed<MINB>, threads, Geo<6>::bytes) !=
+	    cudaSuccess)
+		return 1;
+	return n;
+}
+
+int geometry_mixed_ctas_per_sm(int min_blocks, int threads)
+{
+	return min_blocks >= 2 ? mixed_ctas_per_sm<2>(threads) : mixed_ctas_per_sm<1>(threads);
+}
+
+cudaError_t launch_geometry_mixed(int min_blocks, const GeoLaunch &L, cudaStream_t st)
+{
+	if (!L.n_items) return cudaSuccess;
+	/* 128^3 items use the CTA's scratch slot: never more CTAs than slots */
+	uint32_t grid = L.queue ? L.ctas : L.n_items;
+	if (L.big_scratch) grid = std::min(grid, L.big_slots);
+	if (min_blocks >= 2) {
+		cudaError_t e = cudaFuncSetAttribute(k_geometry_mixed<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+						     (int)Geo<6>::bytes);
+		if (e != cudaSuccess) return e;
+		k_geometry_mixed<2><<<grid, L.threads, Geo<6>::bytes, st>>>(L.sets, L.items, L.n_items, L.queue, L.outs,
+									     L.svl, L.vbo, L.ibo, L.lod_max,
+									     L.big_scratch);
+	} else {
+		cudaError_t e = cudaFuncSetAttribute(k_geometry_mixed<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+						     (int)Geo<6>::bytes);
+		if (e != cudaSuccess) return e;
+		k_geometry_mixed<1><<<grid, L.threads, Geo<6>::bytes, st>>>(L.sets, L.items, L.n_items, L.queue, L.outs,
+									     L.svl, L.vbo, L.ibo, L.lod_max,
+									     L.big_scratch);
+	}
+	return cudaGetLastError();
+}
 
 size_t geometry_smem_bytes(int root_bitw)
 {

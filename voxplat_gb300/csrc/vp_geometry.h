@@ -27,5 +27,10 @@ size_t shell_words_per_chunk(int root_bitw);
 size_t shell_cols_per_chunk(int root_bitw);
 int geometry_ctas_per_sm(int root_bitw, int threads);
 cudaError_t launch_geometry(int root_bitw, const GeoLaunch &L, cudaStream_t st);
+/* One persistent launch over items of any root size (sets may differ in
+ * root_bitw); min_blocks 2 caps registers for two CTAs per SM, 1 leaves the
+ * 128^3 path its registers. With 128^3 items, grid <= big_slots. */
+int geometry_mixed_ctas_per_sm(int min_blocks, int threads);
+cudaError_t launch_geometry_mixed(int min_blocks, const GeoLaunch &L, cudaStream_t st);
 
 } // namespace vp

@@ -130,3 +130,6 @@ int vpi_world_load(vp_world *w, const VpiChunkSrc *src);
 int vpi_world_shadow_window(vp_world *w, const uint16_t *map, uint64_t map_len, uint64_t base, uint64_t n,
 			    uint32_t shadow_w, const int32_t origin[3]);
 int vpi_world_run(vp_world *w, const WorkItem *items, uint32_t n, int lod_max);
+/* A reference-format stream of n words (terminator included) covering N
+ * voxels with nonzero run lengths. */
+extern "C" int vpi_validate_stream(const uint32_t *s, uint32_t n, uint64_t N);

@@ -15,6 +15,9 @@ VP_MAX_LEVELS = 8
 VP_REBUILD_PERSISTENT = 1
 VP_REBUILD_PLAIN = 2
 VP_REBUILD_GROUP = 4
+VP_REBUILD_GRAPH = 8
+VP_BATCH_MIXED = 0
+VP_BATCH_SPLIT = 1
 
 
 class VoxGpuError(RuntimeError):
@@ -43,6 +46,16 @@ assert RESULT_DTYPE.itemsize == ctypes.sizeof(ChunkResult)
 EDIT_DTYPE = np.dtype([("x", np.int32), ("y", np.int32), ("z", np.int32), ("radius", np.uint32),
                        ("voxel", np.uint8), ("pad", np.uint8, (7,)), ("arrival_s", np.float64)])
 assert EDIT_DTYPE.itemsize == 32
+
+
+class BatchTune(ctypes.Structure):
+    _fields_ = [("strategy", ctypes.c_int), ("min_blocks", ctypes.c_int), ("order", ctypes.c_int),
+                ("ctas", ctypes.c_uint32), ("ms", ctypes.c_float)]
+
+    def as_dict(self):
+        return {"strategy": "mixed" if self.strategy == VP_BATCH_MIXED else "split", "min_blocks": self.min_blocks,
+                "order": "longest_first" if self.order == 0 else "by_root_then_longest", "ctas": self.ctas,
+                "ms": round(float(self.ms), 4)}
 
 
 class ServeStats(ctypes.Structure):
@@ -116,6 +129,20 @@ def load(build_if_missing=True):
         "vp_rle_encode": (I, [V, V, U32, V, U32, ctypes.POINTER(U32)]),
         "vp_rle_decode": (I, [V, V, U32, V, U32, ctypes.POINTER(U32)]),
         "vp_world_kernel_ms": (I, [V, V, I, ctypes.POINTER(U32)]),
+        "vp_batch_create": (I, [V, U32, V, PV]),
+        "vp_batch_destroy": (None, [V]),
+        "vp_batch_upload": (I, [V, V, U64, V, V, V, V, V]),
+        "vp_batch_set_modes": (I, [V, V]),
+        "vp_batch_rebuild": (I, [V, I, ctypes.c_uint]),
+        "vp_batch_finish": (I, [V]),
+        "vp_batch_autotune": (I, [V, I, V, V, ctypes.POINTER(I)]),
+        "vp_batch_set_tune": (I, [V, V]),
+        "vp_batch_get_tune": (I, [V, V]),
+        "vp_batch_results": (I, [V, V, U32]),
+        "vp_batch_read_svl": (I, [V, U64, U64, V]),
+        "vp_batch_read_vbo": (I, [V, U64, U64, V]),
+        "vp_batch_read_ibo": (I, [V, U64, U64, V]),
+        "vp_batch_kernel_ms": (I, [V, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(U32)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -329,3 +356,112 @@ class DeviceWorld:
     def chunk_mesh(self, res, c):
         r = res[c]
         return self.read_vbo(r["vbo_off"], r["vbo_items"]), self.read_ibo(r["ibo_off"], r["ibo_items"])
+
+
+class DeviceBatch:
+    """A batch of standalone chunks (each a 1x1x1 World, any root 8..128)
+    resident on the device (include/voxgpu.h, vp_batch_*)."""
+
+    def __init__(self, ctx, chunk_worlds):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.h = None
+        self.n = len(chunk_worlds)
+        rb = np.array([w.root_bitw for w in chunk_worlds], np.int32)
+        for w in chunk_worlds:
+            assert w.nchunks == 1, "batch members are 1x1x1 sets"
+        self.root_bitw = rb
+        h = ctypes.c_void_p()
+        check(self.lib.vp_batch_create(ctx.h, self.n, _p(rb), ctypes.byref(h)), "vp_batch_create")
+        self.h = h
+        lens = np.array([int(w.len[0]) for w in chunk_worlds], np.uint32)
+        offs = np.zeros(self.n, np.uint64)
+        pieces, o = [], 0
+        for k, w in enumerate(chunk_worlds):
+            s = w.pool[int(w.off[0]):int(w.off[0]) + int(w.len[0])]
+            pad = (-len(s)) % 4
+            pieces.append(s)
+            if pad:
+                pieces.append(np.zeros(pad, np.uint32))
+            offs[k] = o
+            o += len(s) + pad
+        pool = np.ascontiguousarray(np.concatenate(pieces), np.uint32)
+        sh_len = np.array([len(w.shadow) for w in chunk_worlds], np.uint64)
+        sh_off = np.zeros(self.n, np.uint64)
+        sh_off[1:] = np.cumsum(sh_len)[:-1]
+        shadow = np.ascontiguousarray(np.concatenate([w.shadow for w in chunk_worlds]), np.uint16)
+        check(self.lib.vp_batch_upload(self.h, _p(pool), len(pool), _p(offs), _p(lens), _p(shadow), _p(sh_off),
+                                       _p(sh_len)), "vp_batch_upload")
+        self.rle_bytes = int(lens.astype(np.int64).sum()) * 4
+        self.voxels = int(sum(1 << (3 * int(r)) for r in rb))
+
+    def close(self):
+        if self.h:
+            self.lib.vp_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_modes(self, make_mesh):
+        if make_mesh is None:
+            check(self.lib.vp_batch_set_modes(self.h, None), "vp_batch_set_modes")
+        else:
+            m = np.ascontiguousarray(make_mesh, dtype=np.uint8)
+            assert len(m) == self.n
+            check(self.lib.vp_batch_set_modes(self.h, _p(m)), "vp_batch_set_modes")
+
+    def rebuild(self, lod_max=4, mode="graph"):
+        """mode: "graph" (replay the tuned configuration's CUDA graph),
+        "direct" (the tuned configuration launched directly) or "plain"
+        (one launch per chunk)."""
+        flags = {"graph": VP_REBUILD_GRAPH, "direct": VP_REBUILD_PERSISTENT, "plain": VP_REBUILD_PLAIN}[mode]
+        check(self.lib.vp_batch_rebuild(self.h, lod_max, flags), "vp_batch_rebuild")
+
+    def finish(self):
+        check(self.lib.vp_batch_finish(self.h), "vp_batch_finish")
+
+    def autotune(self, lod_max=4):
+        best = BatchTune()
+        tried = (BatchTune * 8)()
+        n = ctypes.c_int(8)
+        check(self.lib.vp_batch_autotune(self.h, lod_max, ctypes.byref(best), tried, ctypes.byref(n)),
+              "vp_batch_autotune")
+        return best.as_dict(), [tried[i].as_dict() for i in range(n.value)]
+
+    def set_tune(self, strategy, min_blocks=2, order=None, ctas=0):
+        t = BatchTune()
+        t.strategy = VP_BATCH_MIXED if strategy == "mixed" else VP_BATCH_SPLIT
+        t.min_blocks = min_blocks
+        t.order = (0 if t.strategy == VP_BATCH_MIXED else 1) if order is None else order
+        t.ctas = ctas
+        check(self.lib.vp_batch_set_tune(self.h, ctypes.byref(t)), "vp_batch_set_tune")
+
+    def results(self):
+        out = np.zeros(self.n, RESULT_DTYPE)
+        check(self.lib.vp_batch_results(self.h, _p(out), self.n), "vp_batch_results")
+        return out
+
+    def chunk_splats(self, res, k):
+        r = res[k]
+        out = np.zeros(int(r["svl_total"]), np.int16)
+        check(self.lib.vp_batch_read_svl(self.h, int(r["svl_off"]), len(out), _p(out)), "vp_batch_read_svl")
+        return out, r["svl_items"].copy()
+
+    def chunk_mesh(self, res, k):
+        r = res[k]
+        v = np.zeros(int(r["vbo_items"]), np.int16)
+        i = np.zeros(int(r["ibo_items"]), np.uint32)
+        check(self.lib.vp_batch_read_vbo(self.h, int(r["vbo_off"]), len(v), _p(v)), "vp_batch_read_vbo")
+        check(self.lib.vp_batch_read_ibo(self.h, int(r["ibo_off"]), len(i), _p(i)), "vp_batch_read_ibo")
+        return v, i
+
+    def kernel_ms(self):
+        """(summed rebuild ms, launches) since the last call."""
+        ms = ctypes.c_double()
+        n = ctypes.c_uint32()
+        check(self.lib.vp_batch_kernel_ms(self.h, ctypes.byref(ms), ctypes.byref(n)), "vp_batch_kernel_ms")
+        return ms.value, n.value
