@@ -248,27 +248,41 @@ def run_ours(args):
         torch.cuda.synchronize()
         plain_ms.append(a_.elapsed_time(b_))
     plain_value = world.nchunks / (float(np.median(plain_ms)) / 1e3)
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers: the caller's world and
+    # its output buffers live in pinned host memory; every step uploads the
+    # world (H2D + device validation), rebuilds, and reads the result
+    # records and all outputs back (D2H)
+    keep = []
+
+    def pinned(a, view):
+        t = torch.from_numpy(np.ascontiguousarray(a).view(view)).pin_memory()
+        keep.append(t)
+        return t.numpy().view(a.dtype)
+
+    pool_h = pinned(world.pool, np.int32)
+    off_h = pinned(world.off, np.int64)
+    len_h = pinned(world.len, np.int32)
+    shadow_h = pinned(world.shadow, np.int16)
+    modes_h = pinned(modes, np.int8)
+    cur = [int(np.max(res[k] + res[n])) * m for k, n, m in
+           (("svl_off", "svl_total", 2), ("vbo_off", "vbo_items", 2), ("ibo_off", "ibo_items", 4))]
+    outs_h = [pinned(np.zeros(c // d + (64 << 10), dt), vw) for c, d, dt, vw in
+              ((cur[0], 2, np.int16, np.int16), (cur[1], 2, np.int16, np.int16), (cur[2], 4, np.uint32, np.int32))]
     e2e_t = []
-    h2d = world.pool.nbytes + world.off.nbytes + world.len.nbytes + world.shadow.nbytes + modes.nbytes
+    h2d = pool_h.nbytes + off_h.nbytes + len_h.nbytes + shadow_h.nbytes + modes_h.nbytes
     d2h = 0
-    for k in range(max(2, min(args.steps, 5))):
+    for k in range(max(3, min(args.steps, 10))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        dw.upload(world)
-        dw.set_modes(modes)
+        dw.upload_arrays(pool_h, off_h, len_h, shadow_h, world.shadow_w)
+        dw.set_modes(modes_h)
         dw.rebuild(LOD_MAX, group=True)
         dw.finish()
         r = dw.results()
-        tot_svl = int(np.max(r["svl_off"] + r["svl_total"])) if len(r) else 0
-        tot_vbo = int(np.max(r["vbo_off"] + r["vbo_items"])) if len(r) else 0
-        tot_ibo = int(np.max(r["ibo_off"] + r["ibo_items"])) if len(r) else 0
-        a = dw.read_svl(0, tot_svl)
-        b = dw.read_vbo(0, tot_vbo)
-        c = dw.read_ibo(0, tot_ibo)
+        used = dw.read_outputs(*outs_h)
         e2e_t.append(time.perf_counter() - t0)
-        d2h = r.nbytes + a.nbytes + b.nbytes + c.nbytes
-    e2e_value = world.nchunks / float(np.median(e2e_t))
+        d2h = r.nbytes + sum(used)
+    e2e_value = world.nchunks / float(np.median(e2e_t[1:]))
     out = {
         "metric": METRIC,
         "value": round(value, 1),
@@ -290,7 +304,8 @@ def run_ours(args):
                   "batched_over_plain": round(value / plain_value, 2)},
         "e2e": {"value": round(e2e_value, 1), "unit": "chunks/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
-                "path": "vp_world_upload + vp_world_rebuild(group) + vp_world_finish + results/arena readback"},
+                "path": "pinned host world -> vp_world_upload -> vp_world_rebuild(group) -> vp_world_finish -> "
+                        "vp_world_results + vp_world_read_outputs -> pinned host buffers"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": ncu_traffic(),
                      "traffic_source": "profiles/k_geometry_config2_world.md (ncu dram__bytes_read+write.sum)",
@@ -306,6 +321,8 @@ def run_ours(args):
         dw.close()
         if not args.skip_edits:
             out["edit_serving"] = edit_serving(ctx)
+        if not args.skip_uneven:
+            out["uneven_batch"] = uneven_batch(ctx)
         if not args.skip_full_scale:
             fs = full_scale(ctx)
             res5, dw5 = fs.pop("_res"), fs.pop("_dw")
@@ -343,6 +360,64 @@ def edit_trace(seed, n, rate, extent_xz, band=(8, 56), rmax=32):
     fill = rng.random(n) < 0.5
     rows[:, 4] = np.where(fill, rng.integers(1, 256, n), 0)
     return gpu.make_edits(rows, arrival)
+
+
+def uneven_batch(ctx, n=4096, seed=3, steps=5):
+    """4096 standalone chunks, roots 32/64/128 in ratio 1:6:1, occupancy
+    log-uniform 0.1%..100% (noise blobs + uniform random voxels), colours
+    1..255; splats LOD 0..4. Batched = the autotuned configuration replayed
+    as a CUDA graph (one persistent launch); plain = one launch per chunk."""
+    from concurrent.futures import ThreadPoolExecutor
+    from voxplat_gb300 import gpu
+    from voxplat_gb300 import worldgen as wg
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max(1, min(16, os.cpu_count() or 1))) as ex:
+        ws = list(ex.map(lambda k: wg.uneven_chunk(seed, k), range(n)))
+    gen_s = time.perf_counter() - t0
+    b = gpu.DeviceBatch(ctx, ws)
+    del ws
+    b.set_modes(None)
+    best, tried = b.autotune(LOD_MAX)
+    ctx.set_timing(True)
+    b.rebuild(LOD_MAX, mode="graph")
+    b.finish()
+    b.kernel_ms()
+    for _ in range(steps):
+        b.rebuild(LOD_MAX, mode="graph")
+    b.finish()
+    g_ms, g_launches = b.kernel_ms()
+    g_ms /= steps
+    b.rebuild(LOD_MAX, mode="plain")
+    b.finish()
+    p_ms, p_launches = b.kernel_ms()
+    ctx.set_timing(False)
+    res = b.results()
+    out_b = int(res["svl_total"].astype(np.int64).sum()) * 2
+    step_b = b.rle_bytes + out_b
+    roots = {str(1 << r): int((b.root_bitw == r).sum()) for r in (5, 6, 7)}
+    eq64 = b.voxels / float(64 ** 3)
+    out = {
+        "workload": "%d standalone chunks, roots 32/64/128 (%s), occupancy log-uniform 0.1%%..100%%, LOD 0..4 splats"
+                    % (n, ":".join(str(v) for v in roots.values())),
+        "roots": roots,
+        "batched_ms": round(g_ms, 3),
+        "batched_chunks_per_s": round(n / (g_ms / 1e3), 1),
+        "batched_chunks64_equiv_per_s": round(eq64 / (g_ms / 1e3), 1),
+        "batched_launches_per_rebuild": g_launches // steps,
+        "plain_ms": round(p_ms, 3),
+        "plain_chunks_per_s": round(n / (p_ms / 1e3), 1),
+        "plain_launches_per_rebuild": p_launches,
+        "batched_over_plain": round(p_ms / g_ms, 2),
+        "tune": best,
+        "tried": tried,
+        "rle_in_mb": round(b.rle_bytes / 1e6, 1),
+        "splats_out_mb": round(out_b / 1e6, 1),
+        "step_gbs": round(step_b / (g_ms / 1e3) / 1e9, 1),
+        "step_frac_of_measured_hbm": round(step_b / (g_ms / 1e3) / 1e9 / peaks()[0], 4),
+        "gen_s": round(gen_s, 2),
+    }
+    b.close()
+    return out
 
 
 def edit_serving(ctx, seconds=2.0, rate=2000.0, seed=4):
@@ -505,6 +580,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-edits", action="store_true", help="skip the edit-serving sub-benchmark")
     ap.add_argument("--skip-full-scale", action="store_true", help="skip the 524288-chunk full-scale rebuild")
+    ap.add_argument("--skip-uneven", action="store_true", help="skip the mixed-root batch sub-benchmark")
     args = ap.parse_args()
     import __graft_entry__
     __graft_entry__.build()

@@ -115,6 +115,12 @@ VP_API int vp_world_rebuild(vp_world *w, int lod_max, unsigned flags);
 VP_API int vp_world_finish(vp_world *w);
 
 VP_API int vp_world_results(vp_world *w, vp_chunk_result *out, uint32_t n);
+/* Copy the used part of the three output arenas (splats, vertices,
+ * indices) into host buffers, with the arena layout the results' offsets
+ * index (a NULL buffer is skipped). used_bytes[] gets each used size;
+ * VP_EOVERFLOW when a buffer is smaller. Pinned buffers copy fastest. */
+VP_API int vp_world_read_outputs(vp_world *w, void *svl, uint64_t svl_bytes, void *vbo, uint64_t vbo_bytes, void *ibo,
+				 uint64_t ibo_bytes, uint64_t used_bytes[3]);
 VP_API int vp_world_read_svl(vp_world *w, uint64_t off, uint64_t n, int16_t *dst);
 VP_API int vp_world_read_vbo(vp_world *w, uint64_t off, uint64_t n, int16_t *dst);
 VP_API int vp_world_read_ibo(vp_world *w, uint64_t off, uint64_t n, uint32_t *dst);

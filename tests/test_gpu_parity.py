@@ -118,3 +118,59 @@ def test_rejects_malformed_streams(ctx):
     broken = wg.World(w.root_bitw, w.max_bitw, bad, w.off, w.len, w.shadow, w.shadow_w, w.shadow_z)
     with pytest.raises(gpu.VoxGpuError):
         gpu.DeviceWorld(ctx, broken)
+
+
+def test_upload_validates_on_device_and_repacks_unaligned_streams(ctx):
+    """Streams are checked on the device (sum of counts, zero counts, the
+    terminator); streams off 16-byte boundaries are repacked; a rejected
+    upload leaves nothing to rebuild, and the next valid upload works."""
+    w = worlds.cave_world(4, (1, 1, 1), seed=8)
+    o = OracleWorld(w)
+    dw = gpu.DeviceWorld(ctx, w)
+    assert worlds.compare_world(dw, o, None, 4) == []
+    cases = []
+    short = w.pool.copy()
+    short[w.off[3]] -= 1                       # counts sum to N - 1
+    cases.append((short, w.len))
+    noterm = w.pool.copy()
+    noterm[w.off[5] + w.len[5] - 1] = 7       # no terminator
+    cases.append((noterm, w.len))
+    lens = w.len.copy()
+    lens[2] = 1                               # a stream of one word
+    cases.append((w.pool, lens))
+    for pool, ln in cases:
+        with pytest.raises(gpu.VoxGpuError):
+            dw.upload_arrays(pool, w.off, ln, w.shadow, w.shadow_w)
+        with pytest.raises(gpu.VoxGpuError):
+            dw.rebuild(lod_max=4)
+    # the same streams shifted by one word: offsets off 16-byte boundaries
+    shifted = np.concatenate([np.zeros(1, np.uint32), w.pool])
+    dw.upload_arrays(shifted, w.off + 1, w.len, w.shadow, w.shadow_w)
+    assert worlds.compare_world(dw, o, np.ones(w.nchunks, np.uint8), 4) == []
+    assert worlds.compare_world(dw, o, None, 4) == []
+
+
+def test_read_outputs_returns_the_arena_layout(ctx):
+    w = worlds.cave_world(5, (1, 1, 1), seed=12)
+    dw = gpu.DeviceWorld(ctx, w)
+    modes = (np.arange(w.nchunks) % 2).astype(np.uint8)
+    dw.set_modes(modes)
+    dw.rebuild(lod_max=4)
+    dw.finish()
+    res = dw.results()
+    svl = np.zeros(1 << 22, np.int16)
+    vbo = np.zeros(1 << 23, np.int16)
+    ibo = np.zeros(1 << 22, np.uint32)
+    used = dw.read_outputs(svl, vbo, ibo)
+    for c in range(w.nchunks):
+        r = res[c]
+        if modes[c]:
+            v, i = dw.chunk_mesh(res, c)
+            assert np.array_equal(vbo[r["vbo_off"]:r["vbo_off"] + r["vbo_items"]], v)
+            assert np.array_equal(ibo[r["ibo_off"]:r["ibo_off"] + r["ibo_items"]], i)
+        else:
+            g, _ = dw.chunk_splats(res, c)
+            assert np.array_equal(svl[r["svl_off"]:r["svl_off"] + r["svl_total"]], g)
+    assert used[0] >= int(np.max(res["svl_off"] + res["svl_total"])) * 2
+    with pytest.raises(gpu.VoxGpuError):
+        dw.read_outputs(svl[:16], vbo, ibo)

@@ -228,6 +228,7 @@ VP_API void vp_world_destroy(vp_world *w)
 	dev_free(w->d_shell_bits);
 	dev_free(w->d_shell_col);
 	dev_free(w->d_big);
+	dev_free(w->d_check);
 	dev_free(w->d_set);
 	dev_free(w->d_items);
 	dev_free(w->d_outs);
@@ -294,38 +295,74 @@ VP_API int vp_world_upload(vp_world *w, const uint32_t *pool, uint64_t pool_word
 {
 	if (!w || !pool || !off || !len || (!shadow && shadow_len)) return VP_EINVAL;
 	const uint64_t N = 1ull << (3 * w->root_bitw);
-	/* validate and repack into a 16-byte aligned pool */
-	std::vector<uint64_t> noff(w->nchunks);
-	uint64_t total = 0;
+	/* streams already on 16-byte boundaries are copied as laid out;
+	 * otherwise they are repacked */
+	bool aligned = true;
 	for (uint32_t c = 0; c < w->nchunks; c++) {
-		if (off[c] + len[c] > pool_words) return VP_EINVAL;
-		int rc = vpi_validate_stream(pool + off[c], len[c], N);
-		if (rc) return rc;
-		noff[c] = total;
-		total += (len[c] + 3u) & ~3u;
+		if (len[c] < 2 || off[c] + len[c] > pool_words) return VP_EINVAL;
+		if (off[c] & 3u) aligned = false;
 	}
-	total += 8; /* vector loads may read up to 7 words past a terminator */
-	std::vector<uint32_t> packed(total, 0u);
-	for (uint32_t c = 0; c < w->nchunks; c++)
-		memcpy(&packed[noff[c]], pool + off[c], (size_t)len[c] * sizeof(uint32_t));
+	std::vector<uint64_t> noff;
+	std::vector<uint32_t> packed;
+	const uint32_t *src = pool;
+	const uint64_t *src_off = off;
+	uint64_t words = pool_words;
+	if (!aligned) {
+		noff.resize(w->nchunks);
+		uint64_t total = 0;
+		for (uint32_t c = 0; c < w->nchunks; c++) {
+			noff[c] = total;
+			total += (len[c] + 3u) & ~3u;
+		}
+		packed.assign(total, 0u);
+		for (uint32_t c = 0; c < w->nchunks; c++)
+			memcpy(&packed[noff[c]], pool + off[c], (size_t)len[c] * sizeof(uint32_t));
+		src = packed.data();
+		src_off = noff.data();
+		words = total;
+	}
+	const uint64_t total = words + 8; /* vector loads may read up to 7 words past a terminator */
 	CK(cudaSetDevice(w->ctx->device));
-	CK(cudaStreamSynchronize(w->ctx->stream));
-	dev_free(w->d_pool);
-	dev_free(w->d_shadow);
-	int rc;
-	/* headroom at the tail for streams re-encoded by edits */
-	const uint64_t cap = total + total / 4 + (16u << 20);
-	if ((rc = dev_alloc(&w->d_pool, cap))) return rc;
-	if ((rc = dev_alloc(&w->d_shadow, shadow_len + 8))) return rc;
 	cudaStream_t st = w->ctx->stream;
-	CK(cudaMemcpyAsync(w->d_pool, packed.data(), total * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-	w->pool_cap = cap;
+	CK(cudaStreamSynchronize(st));
+	int rc;
+	/* reuse the allocations when they fit; keep headroom at the pool's tail
+	 * for streams re-encoded by edits */
+	if (!w->d_pool || w->pool_cap < total) {
+		dev_free(w->d_pool);
+		w->pool_cap = 0;
+		const uint64_t cap = total + total / 4 + (16u << 20);
+		if ((rc = dev_alloc(&w->d_pool, cap))) return rc;
+		w->pool_cap = cap;
+	}
+	if (!w->d_shadow || w->shadow_cap < shadow_len + 8) {
+		dev_free(w->d_shadow);
+		w->shadow_cap = 0;
+		if ((rc = dev_alloc(&w->d_shadow, shadow_len + 8))) return rc;
+		w->shadow_cap = shadow_len + 8;
+	}
+	if (!w->d_check && (rc = dev_alloc(&w->d_check, 2))) return rc;
+	CK(cudaMemcpyAsync(w->d_pool, src, words * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+	CK(cudaMemsetAsync(w->d_pool + words, 0, 8 * sizeof(uint32_t), st));
 	w->pool_tail = total;
-	CK(cudaMemcpyAsync(w->d_off, noff.data(), w->nchunks * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+	CK(cudaMemcpyAsync(w->d_off, src_off, w->nchunks * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
 	CK(cudaMemcpyAsync(w->d_len, len, w->nchunks * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-	CK(cudaMemsetAsync(w->d_shadow, 0, (shadow_len + 8) * sizeof(uint16_t), st));
 	if (shadow_len)
 		CK(cudaMemcpyAsync(w->d_shadow, shadow, shadow_len * sizeof(uint16_t), cudaMemcpyHostToDevice, st));
+	CK(cudaMemsetAsync(w->d_shadow + shadow_len, 0, 8 * sizeof(uint16_t), st));
+	/* every stream checked on the device before any kernel decodes it */
+	CK(cudaMemsetAsync(w->d_check, 0, sizeof(uint32_t), st));
+	CK(cudaMemsetAsync(w->d_check + 1, 0xFF, sizeof(uint32_t), st));
+	cudaError_t e = launch_validate_streams(w->d_pool, w->d_off, w->d_len, w->nchunks, N, w->d_check,
+						w->d_check + 1, st);
+	if (e != cudaSuccess) return cuda_fail(e, "stream validation");
+	uint32_t chk[2];
+	CK(cudaMemcpyAsync(chk, w->d_check, sizeof(chk), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	if (chk[0]) {
+		w->uploaded = false;
+		return VP_EINVAL;
+	}
 	w->pool_words = total;
 	w->hlen.assign(len, len + w->nchunks);
 	w->items_dirty = true;
@@ -356,7 +393,9 @@ VP_API int vp_world_generate(vp_world *w, int kind, uint64_t seed, int hshift, u
 	dev_free(w->d_pool);
 	int rc;
 	const uint64_t slen = (uint64_t)a.shadow_w * (Z + pad_rows);
+	w->shadow_cap = 0;
 	if ((rc = dev_alloc(&w->d_shadow, slen + 8))) return rc;
+	w->shadow_cap = slen + 8;
 	CK(cudaMemsetAsync(w->d_shadow, 0, (slen + 8) * 2u, st));
 	/* pool: a first guess, grown (with copy) when a slab does not fit */
 	uint64_t cap = (uint64_t)w->nchunks * 2048u + (uint64_t)nslab * (N + 8u) + (1u << 20);
@@ -665,6 +704,31 @@ VP_API int vp_world_finish(vp_world *w)
 	return VP_EOVERFLOW;
 }
 
+VP_API int vp_world_read_outputs(vp_world *w, void *svl, uint64_t svl_bytes, void *vbo, uint64_t vbo_bytes, void *ibo,
+				 uint64_t ibo_bytes, uint64_t used_bytes[3])
+{
+	if (!w || !used_bytes) return VP_EINVAL;
+	cudaStream_t st = w->ctx->stream;
+	unsigned long long cur[3];
+	CK(cudaMemcpyAsync(cur, w->d_cursors, sizeof(cur), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	void *dst[3] = {svl, vbo, ibo};
+	const uint64_t cap[3] = {svl_bytes, vbo_bytes, ibo_bytes};
+	int rc = VP_OK;
+	for (int a = 0; a < 3; a++) {
+		used_bytes[a] = (uint64_t)cur[a] * 16u;
+		if (cur[a] > w->cap[a]) return VP_EOVERFLOW; /* an unfinished, overflowed rebuild */
+		if (!dst[a] || !used_bytes[a]) continue;
+		if (used_bytes[a] > cap[a]) {
+			rc = VP_EOVERFLOW;
+			continue;
+		}
+		CK(cudaMemcpyAsync(dst[a], w->d_arena[a], used_bytes[a], cudaMemcpyDeviceToHost, st));
+	}
+	CK(cudaStreamSynchronize(st));
+	return rc;
+}
+
 VP_API int vp_world_results(vp_world *w, vp_chunk_result *out, uint32_t n)
 {
 	static_assert(sizeof(vp_chunk_result) == sizeof(ChunkOut), "result record layout");
@@ -840,7 +904,9 @@ int vpi_world_shadow_window(vp_world *w, const uint16_t *map, uint64_t map_len, 
 	CK(cudaStreamSynchronize(st));
 	dev_free(w->d_shadow);
 	int rc;
+	w->shadow_cap = 0;
 	if ((rc = dev_alloc(&w->d_shadow, n + 8u))) return rc;
+	w->shadow_cap = n + 8u;
 	if (n && map) CK(cudaMemcpyAsync(w->d_shadow, map + base, n * sizeof(uint16_t), cudaMemcpyHostToDevice, st));
 	w->shadow_len = n;
 	w->shadow_base = base;

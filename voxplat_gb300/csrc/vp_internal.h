@@ -59,6 +59,8 @@ struct vp_world {
 	uint32_t *d_len = nullptr;
 	uint16_t *d_shadow = nullptr;
 	uint64_t shadow_len = 0;
+	uint64_t shadow_cap = 0;                 /* elements allocated in d_shadow */
+	uint32_t *d_check = nullptr;             /* upload validation: status, first bad chunk */
 	uint32_t shadow_w = 0;
 	uint64_t *d_shell_bits = nullptr;
 	uint8_t *d_shell_col = nullptr;

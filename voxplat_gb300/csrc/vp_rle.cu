@@ -479,4 +479,46 @@ cudaError_t launch_rle_encode_tiles(const uint8_t *vox, uint32_t n, uint32_t N, 
 	return cudaGetLastError();
 }
 
+/* One warp per stream: at least two words, a zero terminator, no zero
+ * count before it, counts summing to N (the checks a stream must pass before
+ * the decoders see it). Failing streams OR kStatusBadStream into *status and
+ * record the lowest failing chunk in *first_bad. */
+__global__ void __launch_bounds__(256) k_validate_streams(const uint32_t *__restrict__ pool,
+							  const uint64_t *__restrict__ off,
+							  const uint32_t *__restrict__ len, uint32_t nchunks, uint64_t N,
+							  uint32_t *status, uint32_t *first_bad)
+{
+	const uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+	const int lane = threadIdx.x & 31;
+	if (c >= nchunks) return;
+	const uint32_t n = len[c];
+	const uint32_t *s = pool + off[c];
+	bool bad = n < 2;
+	uint64_t sum = 0;
+	if (!bad) {
+		bool zero = false;
+		for (uint32_t i = lane; i + 1 < n; i += 32) {
+			const uint32_t cnt = __ldg(s + i) & 0xFFFFFFu;
+			zero |= cnt == 0;
+			sum += cnt;
+		}
+#pragma unroll
+		for (int d = 16; d; d >>= 1) sum += __shfl_xor_sync(kFull, sum, d);
+		zero = __any_sync(kFull, zero);
+		bad = zero || sum != N || __ldg(s + n - 1) != 0;
+	}
+	if (bad && lane == 0) {
+		atomicOr(status, kStatusBadStream);
+		atomicMin(first_bad, c);
+	}
+}
+
+cudaError_t launch_validate_streams(const uint32_t *pool, const uint64_t *off, const uint32_t *len, uint32_t nchunks,
+				    uint64_t N, uint32_t *status, uint32_t *first_bad, cudaStream_t st)
+{
+	if (!nchunks) return cudaSuccess;
+	k_validate_streams<<<(nchunks + 7) / 8, 256, 0, st>>>(pool, off, len, nchunks, N, status, first_bad);
+	return cudaGetLastError();
+}
+
 } // namespace vp

@@ -28,6 +28,12 @@ cudaError_t launch_rle_encode_tiles(const uint8_t *vox, uint32_t n, uint32_t N, 
 				    unsigned long long *cursor, uint64_t *out_off, uint32_t *out_len, uint32_t *status,
 				    uint32_t *tile_scratch, uint32_t *nruns, uint32_t *run_scratch, cudaStream_t st);
 
+/* Check every stream on the device (status |= kStatusBadStream and
+ * first_bad = lowest failing chunk); status and first_bad are set by the
+ * caller (0 and ~0). */
+cudaError_t launch_validate_streams(const uint32_t *pool, const uint64_t *off, const uint32_t *len, uint32_t nchunks,
+				    uint64_t N, uint32_t *status, uint32_t *first_bad, cudaStream_t st);
+
 /* dst[noff[c] ..] = src[off[c] ..], len[c] words, for every chunk c. */
 cudaError_t launch_copy_streams(const uint32_t *src, const uint64_t *off, const uint32_t *len, const uint64_t *noff,
 				uint32_t *dst, uint32_t nchunks, cudaStream_t st);

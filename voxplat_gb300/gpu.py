@@ -114,6 +114,7 @@ def load(build_if_missing=True):
         "vp_world_finish": (I, [V]),
         "vp_world_reserve": (I, [V, V]),
         "vp_world_results": (I, [V, V, U32]),
+        "vp_world_read_outputs": (I, [V, V, U64, V, U64, V, U64, V]),
         "vp_world_read_svl": (I, [V, U64, U64, V]),
         "vp_world_read_vbo": (I, [V, U64, U64, V]),
         "vp_world_read_ibo": (I, [V, U64, U64, V]),
@@ -238,8 +239,12 @@ class DeviceWorld:
         return dw
 
     def upload(self, world):
-        check(self.lib.vp_world_upload(self.h, _p(world.pool), len(world.pool), _p(world.off), _p(world.len),
-                                       _p(world.shadow), len(world.shadow), world.shadow_w), "vp_world_upload")
+        self.upload_arrays(world.pool, world.off, world.len, world.shadow, world.shadow_w)
+
+    def upload_arrays(self, pool, off, lens, shadow, shadow_w):
+        """vp_world_upload from host arrays (pinned ones copy fastest)."""
+        check(self.lib.vp_world_upload(self.h, _p(pool), len(pool), _p(off), _p(lens), _p(shadow), len(shadow),
+                                       shadow_w), "vp_world_upload")
 
     def close(self):
         if self.h:
@@ -288,6 +293,14 @@ class DeviceWorld:
         out = np.zeros(self.nchunks, RESULT_DTYPE)
         check(self.lib.vp_world_results(self.h, _p(out), self.nchunks), "vp_world_results")
         return out
+
+    def read_outputs(self, svl, vbo, ibo):
+        """Copy the used part of the three output arenas into the given
+        arrays (pinned ones copy fastest); returns the used bytes of each."""
+        used = np.zeros(3, np.uint64)
+        check(self.lib.vp_world_read_outputs(self.h, _p(svl), svl.nbytes, _p(vbo), vbo.nbytes, _p(ibo), ibo.nbytes,
+                                             _p(used)), "vp_world_read_outputs")
+        return [int(u) for u in used]
 
     def read_svl(self, off, n):
         out = np.zeros(int(n), np.int16)
