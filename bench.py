@@ -126,16 +126,8 @@ class ClockSampler:
 
 
 def dist_setup():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    if ws <= 1:
-        return 0, 1, None
-    import torch
-    import torch.distributed as dist
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist.init_process_group("nccl")
-    return rank, ws, dist
+    from voxplat_gb300 import replicas
+    return replicas.init("nccl")
 
 
 def cpu_baseline(world, modes, budget_s=12.0, threads=None):
@@ -218,13 +210,9 @@ def run_ours(args):
     step_ms = [s_.elapsed_time(e_) for s_, e_ in zip(starts, ends)]
     shell_ms, geo_ms, grp_ms, launches = dw.kernel_ms()
     ctx.set_timing(False)
-    t_ms = float(np.sum(step_ms))
-    if dist:
-        tt = torch.tensor([t_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_ms = float(tt.item())
-    chunks = world.nchunks * args.steps * ws
-    value = chunks / (t_ms / 1e3)
+    from voxplat_gb300 import replicas
+    t_ms = replicas.max_over_ranks(float(np.sum(step_ms)), dist, device="cuda")
+    value = replicas.whole_job_rate(world.nchunks * args.steps, ws, t_ms)
     ab, rle_b, out_b, sh_b = algorithmic_bytes(world, res)
     geo_avg_ms = geo_ms / args.steps
     peak, peak_kind = peaks()
@@ -340,9 +328,7 @@ def run_ours(args):
             out["full_scale"] = fs
         out["cpu_baseline"] = cpu_baseline(world, modes)
         print(json.dumps(out), flush=True)
-    if dist:
-        dist.barrier()
-        dist.destroy_process_group()
+    replicas.finish(dist)
 
 
 def edit_trace(seed, n, rate, extent_xz, band=(8, 56), rmax=32):
