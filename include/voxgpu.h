@@ -214,6 +214,23 @@ VP_API int vp_rebuild_noalloc(int device, void *stream, int root_bitw, const int
 			      int16_t *vbo, uint64_t vbo_bytes, uint32_t *ibo, uint64_t ibo_bytes,
 			      vp_chunk_result *results);
 
+/* Draw culling and LOD selection of the last rebuild made with
+ * VP_REBUILD_GROUP (octree_cull, src/game.c:319-395, started from LOD
+ * top_lod over the roots of src/game.c:517-524; frustum planes of
+ * src/gfx/fcull.c from the column-major view-projection matrix). The walk's
+ * draw queues, in its order: chunks whose mesh is drawn (chunk index) and
+ * octree nodes whose grouped splats are drawn (lod << 24 | node index, node
+ * numbered as in vp_world_group_nodes). *n_mesh / *n_svl get the queue
+ * lengths; VP_EOVERFLOW when a capacity is short. top_lod must not exceed
+ * the grouped LOD. */
+VP_API int vp_world_cull(vp_world *w, const float view_proj[16], const float lod_origin[3], int top_lod,
+			 uint32_t *mesh_out, uint32_t mesh_cap, uint32_t *n_mesh, uint32_t *svl_out, uint32_t svl_cap,
+			 uint32_t *n_svl);
+/* Mesh-or-splat mode of every chunk from the LOD origin (make_mesh =
+ * chunk centre within 512 voxels, src/game.c:612-625), computed on the
+ * device and applied to the next rebuild; make_mesh_out (optional) gets it. */
+VP_API int vp_world_camera_modes(vp_world *w, const float lod_origin[3], uint8_t *make_mesh_out);
+
 /* Kernel timing: with timing on, every rebuild records CUDA events around
  * its passes on the context stream; vp_world_kernel_ms waits for the stream
  * and returns the summed milliseconds since the last call of ms[0] the shell

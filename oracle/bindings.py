@@ -46,6 +46,12 @@ def vpo_lib():
         lib.vpo_rebuild.argtypes = [V, V, ctypes.c_uint32, V, ctypes.c_int, ctypes.c_int]
         lib.vpo_group_node.restype = ctypes.c_uint64
         lib.vpo_group_node.argtypes = [V, ctypes.c_int, V, V, V, V]
+        lib.vpo_fcull_extract_planes.argtypes = [V, V]
+        lib.vpo_fcull_visible.restype = ctypes.c_int
+        lib.vpo_fcull_visible.argtypes = [V, V, ctypes.c_float]
+        lib.vpo_octree_cull.restype = ctypes.c_uint64
+        lib.vpo_octree_cull.argtypes = [ctypes.c_int, V, V, V, ctypes.c_int, V, V, V, V, V, V]
+        lib.vpo_mesh_flags.argtypes = [ctypes.c_int, V, V, V]
         _vpo = lib
     return _vpo
 
@@ -245,3 +251,92 @@ def vpo_rle_decode(words, n):
     out = np.zeros(n, np.uint8)
     vpo_lib().vpo_rle_decode(_vp(words), _vp(out), n)
     return out
+
+
+# ---------------------------------------------------------------------------
+# draw culling and LOD selection (src/gfx/fcull.c, src/game.c:319-395, 612-625)
+
+def fcull_extract_planes(m):
+    m = np.ascontiguousarray(m, np.float32).reshape(16)
+    out = np.zeros(24, np.float32)
+    vpo_lib().vpo_fcull_extract_planes(_vp(m), _vp(out))
+    return out
+
+
+def fcull_visible(planes, loc, radius):
+    planes = np.ascontiguousarray(planes, np.float32)
+    loc = np.ascontiguousarray(loc, np.float32)
+    return vpo_lib().vpo_fcull_visible(_vp(planes), _vp(loc), float(np.float32(radius)))
+
+
+def ref_fcull_extract_planes(m):
+    """The reference's own gfx_fcull_extract_planes (None without the tree)."""
+    lib = ref_lib()
+    if lib is None:
+        return None
+    m = np.ascontiguousarray(m, np.float32).reshape(16)
+    out = np.zeros(24, np.float32)
+    f = lib.gfx_fcull_extract_planes
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    f(_vp(m), _vp(out))
+    return out
+
+
+def ref_fcull_visible(planes, loc, radius):
+    lib = ref_lib()
+    if lib is None:
+        return None
+    f = lib.gfx_fcull_visible
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float]
+    planes = np.ascontiguousarray(planes, np.float32)
+    loc = np.ascontiguousarray(loc, np.float32)
+    return f(_vp(planes), _vp(loc), float(np.float32(radius)))
+
+
+def octree_cull(root_bitw, max_bitw, planes, origin, has_mesh, svl_items, top=4):
+    """Draw queues of the octree walk: (mesh chunk indices, svl entries
+    lod << 24 | node, nodes visited). svl_items[lod] = items per node."""
+    mb = np.array(max_bitw, np.int32)
+    planes = np.ascontiguousarray(planes, np.float32)
+    origin = np.ascontiguousarray(origin, np.float32)
+    has_mesh = np.ascontiguousarray(has_mesh, np.uint8)
+    n = 1 << int(mb.sum())
+    rows = [np.ascontiguousarray(svl_items[l], np.uint32) for l in range(top + 1)]
+    ptrs = (ctypes.c_void_p * len(rows))(*[r.ctypes.data for r in rows])
+    mesh_out = np.zeros(n, np.uint32)
+    svl_out = np.zeros(2 * n + 64, np.uint32)
+    nm = np.zeros(1, np.uint32)
+    ns = np.zeros(1, np.uint32)
+    visits = vpo_lib().vpo_octree_cull(int(root_bitw), _vp(mb), _vp(planes), _vp(origin), top, _vp(has_mesh),
+                                       ctypes.cast(ptrs, ctypes.c_void_p), _vp(mesh_out), _vp(nm), _vp(svl_out),
+                                       _vp(ns))
+    return mesh_out[:int(nm[0])].copy(), svl_out[:int(ns[0])].copy(), int(visits)
+
+
+def mesh_flags(root_bitw, max_bitw, origin):
+    mb = np.array(max_bitw, np.int32)
+    origin = np.ascontiguousarray(origin, np.float32)
+    out = np.zeros(1 << int(mb.sum()), np.uint8)
+    vpo_lib().vpo_mesh_flags(int(root_bitw), _vp(mb), _vp(origin), _vp(out))
+    return out
+
+
+def perspective_view(eye, target, fov_deg=70.0, aspect=16 / 9, near=0.1, far=16384.0):
+    """A column-major view-projection matrix (float32[16]) for tests."""
+    eye = np.asarray(eye, np.float64)
+    f = np.asarray(target, np.float64) - eye
+    f /= np.linalg.norm(f)
+    up = np.array([0.0, 1.0, 0.0])
+    s = np.cross(f, up)
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    view = np.eye(4)
+    view[0, :3], view[1, :3], view[2, :3] = s, u, -f
+    view[:3, 3] = -view[:3, :3] @ eye
+    t = 1.0 / np.tan(np.radians(fov_deg) / 2)
+    proj = np.zeros((4, 4))
+    proj[0, 0], proj[1, 1] = t / aspect, t
+    proj[2, 2], proj[2, 3] = (far + near) / (near - far), 2 * far * near / (near - far)
+    proj[3, 2] = -1.0
+    return (proj @ view).astype(np.float32).T.reshape(16).copy()

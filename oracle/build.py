@@ -39,6 +39,7 @@ def build_ref(force=False):
         return None
     srcs = [script, os.path.join(HERE, "ref_harness.c"),
             os.path.join(HERE, "refshim", "ref_stubs.c")]
+    srcs.append(os.path.join(ref, "src", "gfx", "fcull.c"))
     if force or _stale(LIBREF, srcs):
         subprocess.check_call(["sh", script], stdout=subprocess.DEVNULL)
     return LIBREF

@@ -16,6 +16,6 @@ gcc -O2 -std=gnu99 -fcommon -fopenmp -w -fPIC -shared -ffp-contract=off \
 	-Wl,-Bsymbolic -I"$HERE/refshim" -I"$REF/src" \
 	-o "$OUT/libvpref.so" \
 	"$REF/src/chunkset.c" "$REF/src/chunkset/rle.c" \
-	"$REF/src/chunkset/mesher.c" "$REF/src/chunkset/edit.c" \
+	"$REF/src/chunkset/mesher.c" "$REF/src/chunkset/edit.c" "$REF/src/gfx/fcull.c" \
 	"$HERE/refshim/ref_stubs.c" "$HERE/ref_harness.c" -lm
 echo "built $OUT/libvpref.so"

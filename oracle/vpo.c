@@ -588,3 +588,114 @@ uint64_t vpo_rebuild(vpo_world *w, const uint32_t *chunks, uint32_t n, const uin
 	}
 	return total;
 }
+
+/* ------------------------------------------------------------------ */
+/* Draw culling and LOD selection                                      */
+/* ------------------------------------------------------------------ */
+
+/* gfx_fcull_extract_planes (src/gfx/fcull.c:20-35): six planes from the
+ * column-major view-projection matrix, normalised by the length of their
+ * normal (float products and sums, the square root in double). */
+void vpo_fcull_extract_planes(const float *m, float *planes)
+{
+	int n = 0;
+	for (int i = 0; i < 3; i++) {
+		for (int j = 0; j < 4; j++) planes[n++] = m[3 + 4 * j] - m[4 * j + i];
+		for (int j = 0; j < 4; j++) planes[n++] = m[3 + 4 * j] + m[4 * j + i];
+	}
+	for (int p = 0; p < 6; p++) {
+		float *q = planes + 4 * p;
+		const float len = (float)sqrt((double)(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]));
+		for (int k = 0; k < 4; k++) q[k] /= len;
+	}
+}
+
+/* gfx_fcull_visible (src/gfx/fcull.c:38-45) */
+int vpo_fcull_visible(const float *planes, const float *loc, float radius)
+{
+	for (int p = 0; p < 6; p++) {
+		const float *q = planes + 4 * p;
+		if ((q[0] * loc[0]) + (q[1] * loc[1]) + (q[2] * loc[2]) + q[3] < -radius) return 0;
+	}
+	return 1;
+}
+
+static float cull_distance(const float *a, const float *b)
+{
+	const float d0 = b[0] - a[0], d1 = b[1] - a[1], d2 = b[2] - a[2];
+	return sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+}
+
+typedef struct {
+	int root_bitw, max_bitw[3];
+	const float *planes, *origin;
+	const uint8_t *has_mesh;
+	const uint32_t *const *svl_items;
+	uint32_t *mesh_out, *n_mesh, *svl_out, *n_svl;
+	uint64_t visits;
+} cull_ctx;
+
+/* octree_cull (src/game.c:319-395). Level 0 is always a leaf: the
+ * reference recurses below it only for a camera exactly at a chunk centre,
+ * with a wrapped level. */
+static void octree_cull_rec(cull_ctx *c, int lod, uint32_t x, uint32_t y, uint32_t z)
+{
+	c->visits++;
+	const uint32_t ws_root = (uint32_t)(1u << c->root_bitw) << lod;
+	const uint32_t v[3] = {x, y, z};
+	float center[3];
+	for (int i = 0; i < 3; i++) center[i] = (float)(v[i] * ws_root + ws_root / 2);
+	for (int i = 0; i < 3; i++)
+		if ((v[i] << lod) >= (1u << c->max_bitw[i])) return;
+	if (!vpo_fcull_visible(c->planes, center, (float)(ws_root * 0.85))) return;
+	const float distance = cull_distance(c->origin, center);
+	if (lod == 0 || distance > (float)(lod * 1024)) {
+		uint32_t ob[3];
+		for (int i = 0; i < 3; i++) ob[i] = (uint32_t)(c->max_bitw[i] - (lod < c->max_bitw[i] ? lod : c->max_bitw[i]));
+		const uint32_t node = ((z << ob[1] | y) << ob[0]) | x;
+		if (lod == 0) {
+			const uint32_t idx = ((z << c->max_bitw[1] | y) << c->max_bitw[0]) | x;
+			if (c->has_mesh[idx]) {
+				c->mesh_out[(*c->n_mesh)++] = idx;
+				return;
+			}
+		}
+		if (!c->svl_items[lod][node]) return;
+		c->svl_out[(*c->n_svl)++] = ((uint32_t)lod << 24) | node;
+		return;
+	}
+	for (uint32_t nx = 0; nx < 2; nx++)
+		for (uint32_t ny = 0; ny < 2; ny++)
+			for (uint32_t nz = 0; nz < 2; nz++)
+				octree_cull_rec(c, lod - 1, 2 * x + nx, 2 * y + ny, 2 * z + nz);
+}
+
+/* The draw-queue walk of src/game.c:517-524. */
+uint64_t vpo_octree_cull(int root_bitw, const int max_bitw[3], const float *planes, const float *origin, int top,
+			 const uint8_t *has_mesh, const uint32_t *const *svl_items, uint32_t *mesh_out,
+			 uint32_t *n_mesh, uint32_t *svl_out, uint32_t *n_svl)
+{
+	cull_ctx c = {root_bitw, {max_bitw[0], max_bitw[1], max_bitw[2]}, planes, origin, has_mesh, svl_items,
+		      mesh_out, n_mesh, svl_out, n_svl, 0};
+	*n_mesh = *n_svl = 0;
+	const uint32_t rx = ((1u << max_bitw[0]) >> top) + 1, ry = ((1u << max_bitw[1]) >> top) + 1,
+		       rz = ((1u << max_bitw[2]) >> top) + 1;
+	for (uint32_t x = 0; x < rx; x++)
+		for (uint32_t y = 0; y < ry; y++)
+			for (uint32_t z = 0; z < rz; z++) octree_cull_rec(&c, top, x, y, z);
+	return c.visits;
+}
+
+/* make_mesh (src/game.c:612-625): chunk centre within 512 of the LOD origin. */
+void vpo_mesh_flags(int root_bitw, const int max_bitw[3], const float *origin, uint8_t *make_mesh)
+{
+	const uint32_t R = 1u << root_bitw;
+	const uint32_t n = 1u << (max_bitw[0] + max_bitw[1] + max_bitw[2]);
+	for (uint32_t c = 0; c < n; c++) {
+		const uint32_t v[3] = {c & ((1u << max_bitw[0]) - 1u), (c >> max_bitw[0]) & ((1u << max_bitw[1]) - 1u),
+				       c >> (max_bitw[0] + max_bitw[1])};
+		float center[3];
+		for (int i = 0; i < 3; i++) center[i] = (float)((v[i] << root_bitw) + (R / 2));
+		make_mesh[c] = cull_distance(center, origin) < 512;
+	}
+}

@@ -93,6 +93,21 @@ uint64_t vpo_group_node(const vpo_world *w, int lod, const uint32_t node[3],
 /* Timed CPU baseline: the reference's per-chunk mesher work for `chunks`,
  * OpenMP over chunks; returns output bytes. */
 void vpo_world_drop_voxels(vpo_world *w);
+
+/* Draw culling and LOD selection (src/gfx/fcull.c, src/game.c:319-395,
+ * 517-524, 612-625). */
+void vpo_fcull_extract_planes(const float *m, float *planes);
+int vpo_fcull_visible(const float *planes, const float *loc, float radius);
+/* Octree walk from LOD `top` over the roots (x, y, z) < (max >> top) + 1,
+ * x outer: chunks whose mesh is drawn go to mesh_out (chunk index), octree
+ * nodes whose grouped splats are drawn to svl_out (lod << 24 | node index).
+ * has_mesh[c] and svl_items[lod][node] describe the uploaded geometry.
+ * Returns the number of nodes visited. */
+uint64_t vpo_octree_cull(int root_bitw, const int max_bitw[3], const float *planes, const float *origin, int top,
+			 const uint8_t *has_mesh, const uint32_t *const *svl_items, uint32_t *mesh_out,
+			 uint32_t *n_mesh, uint32_t *svl_out, uint32_t *n_svl);
+/* make_mesh per chunk: distance from the chunk centre to origin < 512. */
+void vpo_mesh_flags(int root_bitw, const int max_bitw[3], const float *origin, uint8_t *make_mesh);
 uint64_t vpo_rebuild(vpo_world *w, const uint32_t *chunks, uint32_t n, const uint8_t *make_mesh, int lod_max,
 		     int nthreads);
 

@@ -7,6 +7,7 @@
 #include "vp_rle.h"
 #include "vp_group.h"
 #include "vp_gen.h"
+#include "vp_cull.h"
 
 #include <algorithm>
 #include <cstdio>
@@ -229,6 +230,10 @@ VP_API void vp_world_destroy(vp_world *w)
 	dev_free(w->d_shell_col);
 	dev_free(w->d_big);
 	dev_free(w->d_check);
+	dev_free(w->d_cull_slots);
+	dev_free(w->d_cull_blocks);
+	dev_free(w->d_cull_out);
+	dev_free(w->d_flags);
 	dev_free(w->d_set);
 	dev_free(w->d_items);
 	dev_free(w->d_outs);
@@ -727,6 +732,89 @@ VP_API int vp_world_read_outputs(vp_world *w, void *svl, uint64_t svl_bytes, voi
 	}
 	CK(cudaStreamSynchronize(st));
 	return rc;
+}
+
+static CullArgs cull_args(const vp_world *w, const float *origin, int top)
+{
+	CullArgs a;
+	memset(&a, 0, sizeof(a));
+	for (int i = 0; i < 3; i++) a.origin[i] = origin[i];
+	a.root_bitw = (uint32_t)w->root_bitw;
+	for (int i = 0; i < 3; i++) {
+		a.max_bitw[i] = (uint32_t)w->max_bitw[i];
+		a.roots[i] = ((1u << w->max_bitw[i]) >> top) + 1u;
+	}
+	a.top = (uint32_t)top;
+	for (int l = 0; l < kMaxLevels; l++)
+		for (int i = 0; i < 3; i++) a.nodes[l][i] = 1u << (w->max_bitw[i] - std::min(l, w->max_bitw[i]));
+	a.outs = w->d_outs;
+	a.node_items = w->d_node_items;
+	a.nchunks = w->nchunks;
+	return a;
+}
+
+VP_API int vp_world_cull(vp_world *w, const float view_proj[16], const float lod_origin[3], int top_lod,
+			 uint32_t *mesh_out, uint32_t mesh_cap, uint32_t *n_mesh, uint32_t *svl_out, uint32_t svl_cap,
+			 uint32_t *n_svl)
+{
+	if (!w || !view_proj || !lod_origin || !n_mesh || !n_svl) return VP_EINVAL;
+	if ((mesh_cap && !mesh_out) || (svl_cap && !svl_out)) return VP_EINVAL;
+	/* the drawn nodes' splats are the grouped lists of the last rebuild */
+	if (top_lod < 0 || top_lod > w->grouped_lod || top_lod >= kMaxLevels) return VP_EINVAL;
+	CK(cudaSetDevice(w->ctx->device));
+	cudaStream_t st = w->ctx->stream;
+	CullArgs a = cull_args(w, lod_origin, top_lod);
+	memcpy(a.view_proj, view_proj, sizeof(a.view_proj));
+	const uint64_t nslots = cull_slots(a);
+	const uint64_t nblocks = (nslots + 1023) / 1024;
+	int rc;
+	if (w->cull_slots_cap < nslots) {
+		dev_free(w->d_cull_slots);
+		w->cull_slots_cap = 0;
+		if ((rc = dev_alloc(&w->d_cull_slots, nslots))) return rc;
+		w->cull_slots_cap = nslots;
+	}
+	if (w->cull_blocks_cap < 2 * nblocks) {
+		dev_free(w->d_cull_blocks);
+		w->cull_blocks_cap = 0;
+		if ((rc = dev_alloc(&w->d_cull_blocks, 2 * nblocks))) return rc;
+		w->cull_blocks_cap = 2 * nblocks;
+	}
+	/* the drawn nodes cover every chunk at most once: nchunks entries each */
+	if (!w->d_cull_out && (rc = dev_alloc(&w->d_cull_out, 2 * (size_t)w->nchunks + 2))) return rc;
+	a.slots = w->d_cull_slots;
+	uint32_t *mq = w->d_cull_out, *sq = w->d_cull_out + w->nchunks, *tot = w->d_cull_out + 2 * (size_t)w->nchunks;
+	cudaError_t e = launch_cull(a, w->d_cull_blocks, tot, mq, w->nchunks, sq, w->nchunks, st);
+	if (e != cudaSuccess) return cuda_fail(e, "cull launch");
+	w->launches += 4;
+	uint32_t t[2];
+	CK(cudaMemcpyAsync(t, tot, sizeof(t), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	*n_mesh = t[0];
+	*n_svl = t[1];
+	const uint32_t cm = std::min(t[0], mesh_cap), cs = std::min(t[1], svl_cap);
+	if (cm) CK(cudaMemcpyAsync(mesh_out, mq, cm * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+	if (cs) CK(cudaMemcpyAsync(svl_out, sq, cs * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	return (t[0] > mesh_cap || t[1] > svl_cap) ? VP_EOVERFLOW : VP_OK;
+}
+
+VP_API int vp_world_camera_modes(vp_world *w, const float lod_origin[3], uint8_t *make_mesh_out)
+{
+	if (!w || !lod_origin) return VP_EINVAL;
+	CK(cudaSetDevice(w->ctx->device));
+	cudaStream_t st = w->ctx->stream;
+	int rc;
+	if (!w->d_flags && (rc = dev_alloc(&w->d_flags, w->nchunks))) return rc;
+	const CullArgs a = cull_args(w, lod_origin, 0);
+	cudaError_t e = launch_mesh_flags(a, w->d_flags, st);
+	if (e != cudaSuccess) return cuda_fail(e, "mesh flags");
+	w->launches += 1;
+	CK(cudaMemcpyAsync(w->modes.data(), w->d_flags, w->nchunks, cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	w->items_dirty = true;
+	if (make_mesh_out) memcpy(make_mesh_out, w->modes.data(), w->nchunks);
+	return VP_OK;
 }
 
 VP_API int vp_world_results(vp_world *w, vp_chunk_result *out, uint32_t n)

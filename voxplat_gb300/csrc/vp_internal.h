@@ -61,6 +61,13 @@ struct vp_world {
 	uint64_t shadow_len = 0;
 	uint64_t shadow_cap = 0;                 /* elements allocated in d_shadow */
 	uint32_t *d_check = nullptr;             /* upload validation: status, first bad chunk */
+	/* draw culling */
+	uint32_t *d_cull_slots = nullptr;
+	uint64_t cull_slots_cap = 0;
+	uint32_t *d_cull_blocks = nullptr;
+	uint64_t cull_blocks_cap = 0;
+	uint32_t *d_cull_out = nullptr;          /* [2][nchunks] mesh queue, splat queue; [2] totals after */
+	uint8_t *d_flags = nullptr;
 	uint32_t shadow_w = 0;
 	uint64_t *d_shell_bits = nullptr;
 	uint8_t *d_shell_col = nullptr;

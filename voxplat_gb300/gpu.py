@@ -115,6 +115,8 @@ def load(build_if_missing=True):
         "vp_world_reserve": (I, [V, V]),
         "vp_world_results": (I, [V, V, U32]),
         "vp_world_read_outputs": (I, [V, V, U64, V, U64, V, U64, V]),
+        "vp_world_cull": (I, [V, V, V, I, V, U32, ctypes.POINTER(U32), V, U32, ctypes.POINTER(U32)]),
+        "vp_world_camera_modes": (I, [V, V, V]),
         "vp_world_read_svl": (I, [V, U64, U64, V]),
         "vp_world_read_vbo": (I, [V, U64, U64, V]),
         "vp_world_read_ibo": (I, [V, U64, U64, V]),
@@ -301,6 +303,24 @@ class DeviceWorld:
         check(self.lib.vp_world_read_outputs(self.h, _p(svl), svl.nbytes, _p(vbo), vbo.nbytes, _p(ibo), ibo.nbytes,
                                              _p(used)), "vp_world_read_outputs")
         return [int(u) for u in used]
+
+    def cull(self, view_proj, lod_origin, top_lod=4):
+        """Draw queues of the octree walk: (mesh chunk indices, splat nodes
+        lod << 24 | node)."""
+        vp = np.ascontiguousarray(view_proj, np.float32).reshape(16)
+        org = np.ascontiguousarray(lod_origin, np.float32)
+        mq = np.zeros(self.nchunks, np.uint32)
+        sq = np.zeros(self.nchunks, np.uint32)
+        nm, ns = ctypes.c_uint32(), ctypes.c_uint32()
+        check(self.lib.vp_world_cull(self.h, _p(vp), _p(org), top_lod, _p(mq), len(mq), ctypes.byref(nm), _p(sq),
+                                     len(sq), ctypes.byref(ns)), "vp_world_cull")
+        return mq[:nm.value].copy(), sq[:ns.value].copy()
+
+    def camera_modes(self, lod_origin):
+        org = np.ascontiguousarray(lod_origin, np.float32)
+        out = np.zeros(self.nchunks, np.uint8)
+        check(self.lib.vp_world_camera_modes(self.h, _p(org), _p(out)), "vp_world_camera_modes")
+        return out
 
     def read_svl(self, off, n):
         out = np.zeros(int(n), np.int16)
