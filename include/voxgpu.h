@@ -231,6 +231,22 @@ VP_API int vp_world_cull(vp_world *w, const float view_proj[16], const float lod
  * device and applied to the next rebuild; make_mesh_out (optional) gets it. */
 VP_API int vp_world_camera_modes(vp_world *w, const float lod_origin[3], uint8_t *make_mesh_out);
 
+/* The world file / wire format: a 64-byte header (magic "VPW1", version 1,
+ * root_bitw, max_bitw[3], nchunks, shadow_w, pool_words, shadow_len,
+ * pad_rows), then off[nchunks] (u64), len[nchunks] (u32), the packed
+ * streams (u32, each on a 16-byte boundary) and the u16 shadow map, all
+ * little endian (layout in voxplat_gb300/csrc/vp_io.cu). vp_world_open
+ * creates and uploads a world from a file (streams validated on the device). */
+VP_API int vp_world_save(vp_world *w, const char *path);
+VP_API int vp_world_open(vp_ctx *ctx, const char *path, vp_world **out);
+
+/* Picking rays (chunkset_edit_raycast_until_solid, src/chunkset/edit.c:
+ * 248-314), n at once: origins and vectors n x 3 floats; per ray the first
+ * solid voxel (0 if none within 4095 steps), its coordinates (n x 3) and the
+ * normal of the face entered (n x 3, one nonzero component on a hit). */
+VP_API int vp_world_raycast(vp_world *w, uint32_t n, const float *origins, const float *vectors, uint8_t *voxels,
+			    uint32_t *coords, int8_t *normals);
+
 /* Kernel timing: with timing on, every rebuild records CUDA events around
  * its passes on the context stream; vp_world_kernel_ms waits for the stream
  * and returns the summed milliseconds since the last call of ms[0] the shell

@@ -149,6 +149,18 @@ class OracleWorld(_Base):
     def _mesh(self, c, vbo, nv, ibo, ni):
         self.lib.vpo_make_mesh(self.h, c, _vp(vbo), _vp(nv), _vp(ibo), _vp(ni))
 
+    def raycast(self, origin, vector):
+        """(voxel, coord[3], normal[3]) of chunkset_edit_raycast_until_solid."""
+        o = np.ascontiguousarray(origin, np.float32)
+        v = np.ascontiguousarray(vector, np.float32)
+        coord = np.zeros(3, np.uint32)
+        normal = np.zeros(3, np.int8)
+        f = self.lib.vpo_raycast
+        f.restype = ctypes.c_uint8
+        f.argtypes = [ctypes.c_void_p] * 5
+        hit = f(self.h, _vp(o), _vp(v), _vp(coord), _vp(normal))
+        return int(hit), coord, normal
+
     def rebuild(self, chunks, make_mesh, lod_max, nthreads, cold=True):
         """Timed CPU baseline: reference per-chunk work over `chunks`."""
         chunks = np.ascontiguousarray(chunks, np.uint32)
@@ -214,6 +226,17 @@ class RefWorld(_Base):
 
     def _mesh(self, c, vbo, nv, ibo, ni):
         self.lib.vpref_chunk_mesh(self.h, c, _vp(vbo), _vp(nv), _vp(ibo), _vp(ni))
+
+    def raycast(self, origin, vector):
+        o = np.ascontiguousarray(origin, np.float32)
+        v = np.ascontiguousarray(vector, np.float32)
+        coord = np.zeros(3, np.uint32)
+        normal = np.zeros(3, np.int8)
+        f = self.lib.vpref_raycast
+        f.restype = ctypes.c_uint8
+        f.argtypes = [ctypes.c_void_p] * 5
+        hit = f(self.h, _vp(o), _vp(v), _vp(coord), _vp(normal))
+        return int(hit), coord, normal
 
     def voxels(self, c):
         out = np.zeros(self.R ** 3, np.uint8)

@@ -130,6 +130,18 @@ void vpref_edit_sphere(struct ChunkSet *set, int32_t x, int32_t y, int32_t z, ui
 	chunkset_edit_sphere(set, ws, r, v);
 }
 
+/* The reference's DDA picking ray (src/chunkset/edit.c:248-314). */
+Voxel chunkset_edit_raycast_until_solid(struct ChunkSet *set, float *origin, float *vector, uint32_t *coord,
+					int8_t *normal);
+
+uint8_t vpref_raycast(struct ChunkSet *set, const float *origin, const float *vector, uint32_t *coord, int8_t *normal)
+{
+	float o[3] = {origin[0], origin[1], origin[2]}, v[3] = {vector[0], vector[1], vector[2]};
+	prime_rle(set);
+	normal[0] = normal[1] = normal[2] = 0;
+	return chunkset_edit_raycast_until_solid(set, o, v, coord, normal);
+}
+
 void vpref_chunk_voxels(struct ChunkSet *set, uint32_t c, uint8_t *out)
 {
 	struct ChunkMD *m = &set->chunks[c];

@@ -699,3 +699,41 @@ void vpo_mesh_flags(int root_bitw, const int max_bitw[3], const float *origin, u
 		make_mesh[c] = cull_distance(center, origin) < 512;
 	}
 }
+
+/* chunkset_edit_raycast_until_solid (src/chunkset/edit.c:248-314). Float
+ * DDA; a step moves a coordinate through float, as the reference's
+ * `coord += step` does. Stepping below 0 takes the float->unsigned
+ * conversion of x86-64 (through a 64-bit signed integer, truncated to 32
+ * bits), written out explicitly here so every host computes the same: 0 - 1
+ * gives 0xFFFFFFFF, and 0xFFFFFFFF - 1 rounds to 2^32, which truncates to 0. */
+uint8_t vpo_raycast(vpo_world *w, const float *origin, const float *vector, uint32_t *coord, int8_t *normal)
+{
+	float delta[3], next[3], step[3], t[3][3];
+	normal[0] = normal[1] = normal[2] = 0;
+	for (int i = 0; i < 3; i++) coord[i] = (uint32_t)(int)origin[i];
+	for (int i = 0; i < 3; i++)
+		for (int j = 0; j < 3; j++) t[i][j] = vector[j] / vector[i];
+	for (int i = 0; i < 3; i++) {
+		delta[i] = (float)sqrt((double)(t[i][0] * t[i][0] + t[i][1] * t[i][1] + t[i][2] * t[i][2]));
+		if (vector[i] < 0) {
+			step[i] = -1.0f;
+			next[i] = (origin[i] - (float)coord[i]) * delta[i];
+		} else {
+			step[i] = 1.0f;
+			next[i] = ((float)coord[i] + 1.0f - origin[i]) * delta[i];
+		}
+	}
+	for (int loops = 4096; loops-- > 1;) {
+		int side = 0;
+		for (int j = 1; j < 3; j++)
+			if (next[side] > next[j]) side = j;
+		next[side] += delta[side];
+		coord[side] = (uint32_t)(int64_t)((float)coord[side] + step[side]);
+		const uint8_t v = vpo_world_read(w, coord);
+		if (v > 0) {
+			normal[side] = (-vector[side] > 0) ? 1 : -1;
+			return v;
+		}
+	}
+	return 0;
+}

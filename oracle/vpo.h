@@ -106,6 +106,10 @@ int vpo_fcull_visible(const float *planes, const float *loc, float radius);
 uint64_t vpo_octree_cull(int root_bitw, const int max_bitw[3], const float *planes, const float *origin, int top,
 			 const uint8_t *has_mesh, const uint32_t *const *svl_items, uint32_t *mesh_out,
 			 uint32_t *n_mesh, uint32_t *svl_out, uint32_t *n_svl);
+/* chunkset_edit_raycast_until_solid (src/chunkset/edit.c:248-314): the
+ * first solid voxel along the ray (0 if none within 4095 steps), its
+ * coordinates and the normal of the face entered (normal zeroed first). */
+uint8_t vpo_raycast(vpo_world *w, const float *origin, const float *vector, uint32_t *coord, int8_t *normal);
 /* make_mesh per chunk: distance from the chunk centre to origin < 512. */
 void vpo_mesh_flags(int root_bitw, const int max_bitw[3], const float *origin, uint8_t *make_mesh);
 uint64_t vpo_rebuild(vpo_world *w, const uint32_t *chunks, uint32_t n, const uint8_t *make_mesh, int lod_max,

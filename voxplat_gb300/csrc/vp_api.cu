@@ -8,6 +8,7 @@
 #include "vp_group.h"
 #include "vp_gen.h"
 #include "vp_cull.h"
+#include "vp_raycast.h"
 
 #include <algorithm>
 #include <cstdio>
@@ -234,6 +235,8 @@ VP_API void vp_world_destroy(vp_world *w)
 	dev_free(w->d_cull_blocks);
 	dev_free(w->d_cull_out);
 	dev_free(w->d_flags);
+	dev_free(w->d_runidx);
+	dev_free(w->d_rays);
 	dev_free(w->d_set);
 	dev_free(w->d_items);
 	dev_free(w->d_outs);
@@ -350,6 +353,7 @@ VP_API int vp_world_upload(vp_world *w, const uint32_t *pool, uint64_t pool_word
 	CK(cudaMemcpyAsync(w->d_pool, src, words * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
 	CK(cudaMemsetAsync(w->d_pool + words, 0, 8 * sizeof(uint32_t), st));
 	w->pool_tail = total;
+	w->pool_version++;
 	CK(cudaMemcpyAsync(w->d_off, src_off, w->nchunks * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
 	CK(cudaMemcpyAsync(w->d_len, len, w->nchunks * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
 	if (shadow_len)
@@ -431,6 +435,7 @@ VP_API int vp_world_generate(vp_world *w, int kind, uint64_t seed, int hshift, u
 			if (e != cudaSuccess) break;
 			if (!((uint32_t)h[1] & kStatusOverflow)) {
 				e = launch_scatter_slab(noff, nlen, nslab, cz * nslab, tail, w->d_off, w->d_len, st);
+				w->pool_version++;
 				tail += h[0];
 				break;
 			}
@@ -817,6 +822,57 @@ VP_API int vp_world_camera_modes(vp_world *w, const float lod_origin[3], uint8_t
 	return VP_OK;
 }
 
+VP_API int vp_world_raycast(vp_world *w, uint32_t n, const float *origins, const float *vectors, uint8_t *voxels,
+			    uint32_t *coords, int8_t *normals)
+{
+	if (!w || !w->uploaded || (n && (!origins || !vectors || !voxels || !coords || !normals))) return VP_EINVAL;
+	if (!n) return VP_OK;
+	CK(cudaSetDevice(w->ctx->device));
+	cudaStream_t st = w->ctx->stream;
+	int rc;
+	if (w->runidx_version != w->pool_version) {
+		if (w->runidx_cap < w->pool_cap) {
+			dev_free(w->d_runidx);
+			w->runidx_cap = 0;
+			if ((rc = dev_alloc(&w->d_runidx, w->pool_cap))) return rc;
+			w->runidx_cap = w->pool_cap;
+		}
+		cudaError_t e = launch_run_starts(w->d_pool, w->d_off, w->d_len, w->nchunks, w->d_runidx, st);
+		if (e != cudaSuccess) return cuda_fail(e, "run-start index");
+		w->launches += 1;
+		w->runidx_version = w->pool_version;
+	}
+	/* ray buffers: origins, vectors (12 B each), coords (12 B), voxel, normal (3 B) */
+	const size_t need = (size_t)n * 40u;
+	if (w->rays_cap < need) {
+		dev_free(w->d_rays);
+		w->rays_cap = 0;
+		if ((rc = dev_alloc(&w->d_rays, need))) return rc;
+		w->rays_cap = need;
+	}
+	float *d_o = (float *)w->d_rays, *d_v = d_o + 3 * (size_t)n;
+	uint32_t *d_c = (uint32_t *)(d_v + 3 * (size_t)n);
+	uint8_t *d_vox = (uint8_t *)(d_c + 3 * (size_t)n);
+	int8_t *d_n = (int8_t *)(d_vox + n);
+	CK(cudaMemcpyAsync(d_o, origins, 12u * n, cudaMemcpyHostToDevice, st));
+	CK(cudaMemcpyAsync(d_v, vectors, 12u * n, cudaMemcpyHostToDevice, st));
+	RayWorld W;
+	W.pool = w->d_pool;
+	W.off = w->d_off;
+	W.len = w->d_len;
+	W.runidx = w->d_runidx;
+	W.root_bitw = (uint32_t)w->root_bitw;
+	for (int i = 0; i < 3; i++) W.max_bitw[i] = (uint32_t)w->max_bitw[i];
+	cudaError_t e = launch_raycast(W, d_o, d_v, n, d_vox, d_c, d_n, st);
+	if (e != cudaSuccess) return cuda_fail(e, "raycast");
+	w->launches += 1;
+	CK(cudaMemcpyAsync(voxels, d_vox, n, cudaMemcpyDeviceToHost, st));
+	CK(cudaMemcpyAsync(coords, d_c, 12u * n, cudaMemcpyDeviceToHost, st));
+	CK(cudaMemcpyAsync(normals, d_n, 3u * n, cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	return VP_OK;
+}
+
 VP_API int vp_world_results(vp_world *w, vp_chunk_result *out, uint32_t n)
 {
 	static_assert(sizeof(vp_chunk_result) == sizeof(ChunkOut), "result record layout");
@@ -971,6 +1027,7 @@ int vpi_world_load(vp_world *w, const VpiChunkSrc *src)
 			len[byte_chunks[k]] = elen[k];
 		}
 	}
+	w->pool_version++;
 	CK(cudaMemcpyAsync(w->d_off, off.data(), w->nchunks * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
 	CK(cudaMemcpyAsync(w->d_len, len.data(), w->nchunks * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
 	w->hlen = len;

@@ -68,6 +68,12 @@ struct vp_world {
 	uint64_t cull_blocks_cap = 0;
 	uint32_t *d_cull_out = nullptr;          /* [2][nchunks] mesh queue, splat queue; [2] totals after */
 	uint8_t *d_flags = nullptr;
+	/* picking rays: run-start index of the current pool version */
+	uint64_t pool_version = 0, runidx_version = ~0ull;
+	uint32_t *d_runidx = nullptr;
+	uint64_t runidx_cap = 0;
+	uint8_t *d_rays = nullptr;
+	size_t rays_cap = 0;
 	uint32_t shadow_w = 0;
 	uint64_t *d_shell_bits = nullptr;
 	uint8_t *d_shell_col = nullptr;

@@ -108,6 +108,7 @@ int compact_pool(vp_world *w, uint64_t extra_words)
 	cudaError_t e = cudaMemcpyAsync(d_noff, noff.data(), w->nchunks * 8u, cudaMemcpyHostToDevice, st);
 	if (e == cudaSuccess) e = launch_copy_streams(w->d_pool, w->d_off, w->d_len, d_noff, np, w->nchunks, st);
 	if (e == cudaSuccess) e = cudaMemcpyAsync(w->d_off, d_noff, w->nchunks * 8u, cudaMemcpyDeviceToDevice, st);
+	w->pool_version++;
 	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
 	dev_free(d_noff);
 	if (e != cudaSuccess) {
@@ -273,6 +274,7 @@ int enqueue_batch(vp_world *w, const vp_edit *edits, uint32_t n)
 				    w->d_new_off, w->d_new_len, (uint32_t *)(w->d_edit_sc + 1), w->d_tile_scratch,
 				    w->d_nruns, w->d_run_scratch, st);
 	if (e == cudaSuccess)
+		w->pool_version++;
 		e = launch_scatter_streams(w->d_dirty, nd, w->d_new_off, w->d_new_len, w->pool_tail, w->d_off, w->d_len,
 					   st);
 	if (e != cudaSuccess) return cuda_fail(e, "edit re-encode");

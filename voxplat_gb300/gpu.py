@@ -117,6 +117,9 @@ def load(build_if_missing=True):
         "vp_world_read_outputs": (I, [V, V, U64, V, U64, V, U64, V]),
         "vp_world_cull": (I, [V, V, V, I, V, U32, ctypes.POINTER(U32), V, U32, ctypes.POINTER(U32)]),
         "vp_world_camera_modes": (I, [V, V, V]),
+        "vp_world_raycast": (I, [V, U32, V, V, V, V, V]),
+        "vp_world_save": (I, [V, ctypes.c_char_p]),
+        "vp_world_open": (I, [V, ctypes.c_char_p, PV]),
         "vp_world_read_svl": (I, [V, U64, U64, V]),
         "vp_world_read_vbo": (I, [V, U64, U64, V]),
         "vp_world_read_ibo": (I, [V, U64, U64, V]),
@@ -240,6 +243,19 @@ class DeviceWorld:
         check(dw.lib.vp_world_generate(dw.h, kind, seed, hshift, pad_rows), "vp_world_generate")
         return dw
 
+    @classmethod
+    def open(cls, ctx, path):
+        """A world read from a VPW1 file (vp_world_open)."""
+        h = ctypes.c_void_p()
+        check(ctx.lib.vp_world_open(ctx.h, os.fsencode(path), ctypes.byref(h)), "vp_world_open")
+        with open(path, "rb") as f:
+            hdr = np.frombuffer(f.read(24), np.int32)
+        dw = cls.__new__(cls)
+        dw.ctx, dw.lib, dw.world, dw.h = ctx, ctx.lib, None, h
+        dw.root_bitw, dw.max_bitw = int(hdr[2]), tuple(int(b) for b in hdr[3:6])
+        dw.nchunks = 1 << sum(dw.max_bitw)
+        return dw
+
     def upload(self, world):
         self.upload_arrays(world.pool, world.off, world.len, world.shadow, world.shadow_w)
 
@@ -315,6 +331,22 @@ class DeviceWorld:
         check(self.lib.vp_world_cull(self.h, _p(vp), _p(org), top_lod, _p(mq), len(mq), ctypes.byref(nm), _p(sq),
                                      len(sq), ctypes.byref(ns)), "vp_world_cull")
         return mq[:nm.value].copy(), sq[:ns.value].copy()
+
+    def save(self, path):
+        """Write the world (streams + shadow map) in the VPW1 file format."""
+        check(self.lib.vp_world_save(self.h, os.fsencode(path)), "vp_world_save")
+
+    def raycast(self, origins, vectors):
+        """(voxels[n], coords[n, 3], normals[n, 3]) of n picking rays."""
+        o = np.ascontiguousarray(origins, np.float32).reshape(-1, 3)
+        v = np.ascontiguousarray(vectors, np.float32).reshape(-1, 3)
+        n = len(o)
+        vox = np.zeros(n, np.uint8)
+        coords = np.zeros((n, 3), np.uint32)
+        normals = np.zeros((n, 3), np.int8)
+        check(self.lib.vp_world_raycast(self.h, n, _p(o), _p(v), _p(vox), _p(coords), _p(normals)),
+              "vp_world_raycast")
+        return vox, coords, normals
 
     def camera_modes(self, lod_origin):
         org = np.ascontiguousarray(lod_origin, np.float32)

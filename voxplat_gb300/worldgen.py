@@ -90,6 +90,56 @@ class World:
         o = int(self.off[c])
         return self.pool[o:o + int(self.len[c])]
 
+    FILE_MAGIC = 0x31575056  # "VPW1"
+
+    def save(self, path):
+        """Write the VPW1 world file (layout in csrc/vp_io.cu): header, offset
+        and length tables, the streams packed on 16-byte boundaries, the
+        shadow map; little endian."""
+        n = self.nchunks
+        noff = np.zeros(n, np.uint64)
+        pieces, o = [], 0
+        for c in range(n):
+            s_ = self.chunk_rle(c)
+            pad = (-len(s_)) % 4
+            noff[c] = o
+            pieces.append(s_)
+            if pad:
+                pieces.append(np.zeros(pad, np.uint32))
+            o += len(s_) + pad
+        pool = np.concatenate(pieces).astype("<u4") if pieces else np.zeros(0, "<u4")
+        hdr = np.zeros(16, "<u4")
+        hdr[0], hdr[1], hdr[2] = self.FILE_MAGIC, 1, self.root_bitw
+        hdr[3:6] = self.max_bitw
+        hdr[6], hdr[7] = n, self.shadow_w
+        hdr[8:10] = np.array([len(pool)], "<u8").view("<u4")
+        hdr[10:12] = np.array([len(self.shadow)], "<u8").view("<u4")
+        hdr[12] = self.pad_rows
+        with open(path, "wb") as f:
+            f.write(hdr.tobytes())
+            f.write(noff.astype("<u8").tobytes())
+            f.write(self.len.astype("<u4").tobytes())
+            f.write(pool.tobytes())
+            f.write(self.shadow.astype("<u2").tobytes())
+
+    @classmethod
+    def load(cls, path):
+        """Read a VPW1 world file."""
+        with open(path, "rb") as f:
+            hdr = np.frombuffer(f.read(64), "<u4")
+            if int(hdr[0]) != cls.FILE_MAGIC or int(hdr[1]) != 1:
+                raise ValueError("not a VPW1 world file")
+            rb, mb, n, sw = int(hdr[2]), tuple(int(b) for b in hdr[3:6]), int(hdr[6]), int(hdr[7])
+            pool_words = int(hdr[8:10].view("<u8")[0])
+            shadow_len = int(hdr[10:12].view("<u8")[0])
+            pad = int(hdr[12])
+            off = np.frombuffer(f.read(8 * n), "<u8").astype(np.uint64)
+            lens = np.frombuffer(f.read(4 * n), "<u4").astype(np.uint32)
+            pool = np.frombuffer(f.read(4 * pool_words), "<u4").astype(np.uint32)
+            shadow = np.frombuffer(f.read(2 * shadow_len), "<u2").astype(np.uint16)
+        z = (1 << mb[2]) << rb
+        return cls(rb, mb, pool, off, lens, shadow, sw, z, pad)
+
     def chunk_coords(self, c):
         bx, by, _ = self.max_bitw
         return (c & ((1 << bx) - 1), (c >> bx) & ((1 << by) - 1), c >> (bx + by))
