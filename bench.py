@@ -306,6 +306,7 @@ def run_ours(args):
     }
     if rank == 0:
         out["clocks"] = clk.summary()
+        out["picking"] = picking(dw)
         dw.close()
         if not args.skip_edits:
             out["edit_serving"] = edit_serving(ctx)
@@ -324,6 +325,7 @@ def run_ours(args):
             fs["step_bytes"] = int(ab5)
             fs["step_gbs"] = round(ab5 / (fs["ms_per_rebuild"] / 1e3) / 1e9, 1)
             fs["step_frac_of_measured_hbm"] = round(fs["step_gbs"] / peaks()[0], 4)
+            fs["draw_cull"] = draw_cull(dw5)
             dw5.close()
             out["full_scale"] = fs
         out["cpu_baseline"] = cpu_baseline(world, modes)
@@ -452,6 +454,44 @@ def edit_serving(ctx, seconds=2.0, rate=2000.0, seed=4):
     }
     dw.close()
     return out
+
+
+def draw_cull(dw, reps=20):
+    """Octree draw cull + LOD selection (src/game.c:319-395) of the grouped
+    world from a camera at its centre, through the C ABI (queues to host)."""
+    from voxplat_gb300.camera import perspective_view
+    ext = [(1 << dw.root_bitw) << b for b in dw.max_bitw]
+    eye = np.array([ext[0] / 2, 300.0, ext[2] / 2], np.float32)
+    vp = perspective_view(eye, eye + np.array([0.3, -0.2, 1.0]), fov_deg=70, far=40000)
+    mq, sq = dw.cull(vp, eye)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        mq, sq = dw.cull(vp, eye)
+    ms = (time.perf_counter() - t0) / reps * 1e3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        dw.camera_modes(eye)
+    mm = (time.perf_counter() - t0) / reps * 1e3
+    nodes = sum((dw.nchunks >> (3 * l)) for l in range(5))
+    return {"ms_per_cull": round(ms, 3), "octree_nodes": int(nodes), "mesh_queue": int(len(mq)),
+            "splat_queue": int(len(sq)), "ms_per_camera_modes": round(mm, 3)}
+
+
+def picking(dw, n=65536, seed=6):
+    """Picking rays (chunkset_edit_raycast_until_solid) through the C ABI:
+    n rays from above the terrain, downwards at random angles."""
+    rng = np.random.default_rng(seed)
+    ext = [(1 << dw.root_bitw) << b for b in dw.max_bitw]
+    org = np.stack([rng.uniform(0, ext[0], n), rng.uniform(200, ext[1], n), rng.uniform(0, ext[2], n)], 1)
+    vec = np.stack([rng.normal(size=n), -np.abs(rng.normal(size=n)) - 0.2, rng.normal(size=n)], 1)
+    org, vec = org.astype(np.float32), vec.astype(np.float32)
+    vox, _, _ = dw.raycast(org, vec)
+    t0 = time.perf_counter()
+    for _ in range(5):
+        vox, _, _ = dw.raycast(org, vec)
+    s_ = (time.perf_counter() - t0) / 5
+    return {"rays": n, "ms_per_batch": round(s_ * 1e3, 3), "rays_per_s": round(n / s_, 1),
+            "hit_fraction": round(float((vox > 0).mean()), 3)}
 
 
 def full_scale(ctx, steps=3):

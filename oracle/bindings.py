@@ -345,21 +345,7 @@ def mesh_flags(root_bitw, max_bitw, origin):
     return out
 
 
-def perspective_view(eye, target, fov_deg=70.0, aspect=16 / 9, near=0.1, far=16384.0):
-    """A column-major view-projection matrix (float32[16]) for tests."""
-    eye = np.asarray(eye, np.float64)
-    f = np.asarray(target, np.float64) - eye
-    f /= np.linalg.norm(f)
-    up = np.array([0.0, 1.0, 0.0])
-    s = np.cross(f, up)
-    s /= np.linalg.norm(s)
-    u = np.cross(s, f)
-    view = np.eye(4)
-    view[0, :3], view[1, :3], view[2, :3] = s, u, -f
-    view[:3, 3] = -view[:3, :3] @ eye
-    t = 1.0 / np.tan(np.radians(fov_deg) / 2)
-    proj = np.zeros((4, 4))
-    proj[0, 0], proj[1, 1] = t / aspect, t
-    proj[2, 2], proj[2, 3] = (far + near) / (near - far), 2 * far * near / (near - far)
-    proj[3, 2] = -1.0
-    return (proj @ view).astype(np.float32).T.reshape(16).copy()
+def perspective_view(*args, **kw):
+    """A column-major view-projection matrix (voxplat_gb300.camera)."""
+    from voxplat_gb300.camera import perspective_view as pv
+    return pv(*args, **kw)
