@@ -214,16 +214,16 @@ __device__ void decode_chunk(const uint32_t *__restrict__ s, uint32_t nruns, con
 	const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 	const int seg = (RR + nw - 1) / nw;
 	const int lo = warp * seg, hi = min(RR, lo + seg);
-	uint32_t par = 0, cnt = 0;
-	for (int r = lo + lane; r < hi; r += 32) {
-		par ^= __popcll(m.occ[hidx<RB>(r & (R - 1), r >> RB)]) & 1;
-		cnt += __popcll(m.rs[r]);
-	}
+	/* per row: run starts n (<= 64) and toggle parity p, packed as
+	 * n << 13 | p so that one add-reduction gives both (the low bit of the
+	 * summed parities is their XOR; at most 4096 rows, so the parity sum
+	 * stays below 2^13 and the packed sum below 2^32) */
+	uint32_t acc = 0;
+	for (int r = lo + lane; r < hi; r += 32)
+		acc += ((uint32_t)__popcll(m.rs[r]) << 13) | ((uint32_t)__popcll(m.occ[hidx<RB>(r & (R - 1), r >> RB)]) & 1u);
 #pragma unroll
-	for (int d = 16; d; d >>= 1) {
-		par ^= __shfl_xor_sync(kFull, par, d);
-		cnt += __shfl_xor_sync(kFull, cnt, d);
-	}
+	for (int d = 16; d; d >>= 1) acc += __shfl_xor_sync(kFull, acc, d);
+	const uint32_t par = acc & 1u, cnt = acc >> 13;
 	if (lane == 0) m.tmp[warp] = (cnt << 1) | par;
 	__syncthreads();
 	if (warp == 0) {
@@ -244,16 +244,19 @@ __device__ void decode_chunk(const uint32_t *__restrict__ s, uint32_t nruns, con
 			t = m.occ[hi_];
 			q = m.rs[r];
 		}
-		uint32_t p = __popcll(t) & 1u, n = __popcll(q);
-		uint32_t pi = warp_incl_xor(p), ni = warp_incl_add(n);
+		/* one scan of n << 6 | p: the low 6 bits sum the 32 parities */
+		const uint32_t p = __popcll(t) & 1u, n = __popcll(q);
+		const uint32_t inc = warp_incl_add((n << 6) | p);
+		const uint32_t pi = inc & 1u, ni = inc >> 6;
 		if (r < hi) {
 			uint64_t o = prefix_xor64(t);
 			if (cpar ^ pi ^ p) o = ~o;
 			m.occ[hi_] = o & G::MASK;
 			m.rank[r] = ccnt + ni - n;
 		}
-		cpar ^= __shfl_sync(kFull, pi, 31);
-		ccnt += __shfl_sync(kFull, ni, 31);
+		const uint32_t last = __shfl_sync(kFull, inc, 31);
+		cpar ^= last & 1u;
+		ccnt += last >> 6;
 	}
 	__syncthreads();
 }
@@ -891,7 +894,7 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
  * the chosen child is its highest set bit. */
 template <int RB>
 __device__ __forceinline__ void emit_splat(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m,
-					   const uint32_t cv[3], int l, int x, int y, int z, int16_t *dst)
+					   const uint32_t cv[3], int l, int x, int y, int z, int16_t *dst, bool sh_in)
 {
 	constexpr int R = Geo<RB>::R;
 	int cx = x, cy = y, cz = z;
@@ -920,8 +923,31 @@ __device__ __forceinline__ void emit_splat(const SetDesc &S, const uint32_t *__r
 	const uint32_t wx = (cv[0] << RB) + ((uint32_t)x << l);
 	const uint32_t wy = (cv[1] << RB) + ((uint32_t)y << l);
 	const uint32_t wz = (cv[2] << RB) + ((uint32_t)z << l);
-	const uint32_t shadow = (uint32_t)shadow_sample(S, wx + sh, wy + sh, wz + sh);
+	uint32_t shadow;
+	if (sh_in) {
+		/* the chunk's whole sample window lies inside the map: no bounds
+		 * checks (shadow_sample, src/chunkset/shadow.h:45-63) */
+		const uint32_t lim = wy + sh + 1u;
+		const uint16_t *p = S.shadow + (((uint64_t)((wx + sh) + (wy + sh)) + (uint64_t)S.shadow_w * (wz + sh)) -
+						S.shadow_base);
+		shadow = !((__ldg(p) < lim) & (__ldg(p + 1) < lim));
+	} else {
+		shadow = (uint32_t)shadow_sample(S, wx + sh, wy + sh, wz + sh);
+	}
 	store_splat(dst, wx, wy, wz, colour | (shadow << 6));
+}
+
+/* Whether every shadow sample of a chunk's splats (world coordinates up to
+ * its far corner plus 2^lod_max, and the entry after) falls inside the map
+ * and needs no uint32 wrap. */
+template <int RB>
+__device__ __forceinline__ bool shadow_window_inside(const SetDesc &S, const uint32_t cv[3], int lod_max)
+{
+	const uint64_t ext = (1u << RB) + (1u << lod_max);
+	const uint64_t x0 = (uint64_t)cv[0] << RB, y0 = (uint64_t)cv[1] << RB, z0 = (uint64_t)cv[2] << RB;
+	const uint64_t lo = x0 + y0 + (uint64_t)S.shadow_w * z0;
+	const uint64_t hi = (x0 + ext) + (y0 + ext) + (uint64_t)S.shadow_w * (z0 + ext) + 1u;
+	return hi < (1ull << 32) && lo >= S.shadow_base && hi - S.shadow_base < S.shadow_len;
 }
 
 template <int RB>
@@ -1004,6 +1030,7 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 	__syncthreads();
 	if (!s_ok) return;
 	int16_t *dst = (int16_t *)asvl.base + s_base * 8u;
+	const bool sh_in = shadow_window_inside<RB>(S, cv, lod_max);
 	/* pass 2: warps take groups from a shared counter; one splat per lane
 	 * per step, a second one when the group has more than 32 left */
 	for (;;) {
@@ -1029,29 +1056,26 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 		const uint32_t T = __shfl_sync(kFull, inc, 31);
 		const uint32_t base = m.grp[g];
 		for (uint32_t k = 0; k < T; k += 64) {
-			{
-				const uint32_t j = k + lane;
-				const int s = search_lane(excl, j);
-				const uint32_t e = __shfl_sync(kFull, excl, s), q = __shfl_sync(kFull, yz, s);
-				const uint64_t w = shfl64(row, s);
-				if (j < T) {
-					const int kk = (int)(j - e);
-					const int x = kk < __popcll(w) ? select_bit(w, kk) : R;
-					emit_splat<RB>(S, stream, m, cv, l, x, (int)(q & 0xFFFFu), (int)(q >> 16),
-						       dst + (size_t)(base + j) * 4);
-				}
+			/* two items per lane when more than 32 remain: both searches
+			 * first, so their shuffle chains overlap */
+			const bool two = k + 32 < T;
+			const uint32_t j0 = k + lane, j1 = k + 32 + lane;
+			const int s0 = search_lane(excl, j0);
+			const int s1 = two ? search_lane(excl, j1) : 0;
+			const uint32_t e0 = __shfl_sync(kFull, excl, s0), q0 = __shfl_sync(kFull, yz, s0);
+			const uint32_t e1 = __shfl_sync(kFull, excl, s1), q1 = __shfl_sync(kFull, yz, s1);
+			const uint64_t w0 = shfl64(row, s0), w1 = shfl64(row, s1);
+			if (j0 < T) {
+				const int kk = (int)(j0 - e0);
+				const int x = kk < __popcll(w0) ? select_bit(w0, kk) : R;
+				emit_splat<RB>(S, stream, m, cv, l, x, (int)(q0 & 0xFFFFu), (int)(q0 >> 16),
+					       dst + (size_t)(base + j0) * 4, sh_in);
 			}
-			if (k + 32 < T) {
-				const uint32_t j = k + 32 + lane;
-				const int s = search_lane(excl, j);
-				const uint32_t e = __shfl_sync(kFull, excl, s), q = __shfl_sync(kFull, yz, s);
-				const uint64_t w = shfl64(row, s);
-				if (j < T) {
-					const int kk = (int)(j - e);
-					const int x = kk < __popcll(w) ? select_bit(w, kk) : R;
-					emit_splat<RB>(S, stream, m, cv, l, x, (int)(q & 0xFFFFu), (int)(q >> 16),
-						       dst + (size_t)(base + j) * 4);
-				}
+			if (two && j1 < T) {
+				const int kk = (int)(j1 - e1);
+				const int x = kk < __popcll(w1) ? select_bit(w1, kk) : R;
+				emit_splat<RB>(S, stream, m, cv, l, x, (int)(q1 & 0xFFFFu), (int)(q1 >> 16),
+					       dst + (size_t)(base + j1) * 4, sh_in);
 			}
 		}
 	}
