@@ -247,6 +247,26 @@ VP_API int vp_world_open(vp_ctx *ctx, const char *path, vp_world **out);
 VP_API int vp_world_raycast(vp_world *w, uint32_t n, const float *origins, const float *vectors, uint8_t *voxels,
 			    uint32_t *coords, int8_t *normals);
 
+/* Headless rasteriser for the drawn geometry (resources/splat.vert.glsl,
+ * splat.frag.glsl, mesh.vert.glsl, mesh.frag.glsl restated in CUDA): the
+ * splats of the drawn octree nodes (svl_queue entries lod << 24 | node, the
+ * grouped lists of the last VP_REBUILD_GROUP rebuild) and the meshes of the
+ * drawn chunks (mesh_queue), e.g. vp_world_cull's queues. Matrices are
+ * column-major. rgba gets width x height RGBA8 words (row 0 at the bottom),
+ * depth (optional) the depth values. stats (optional, 4 values): splats and
+ * triangles submitted, splats and triangles rasterised by whole blocks
+ * (footprint above 256 pixels). */
+typedef struct vp_camera {
+	float projection[16], view_rotation[16], view_translation[16];
+	float view_projection[16];   /* projection x view_rotation x view_translation */
+	float inv_proj_view_rot[16]; /* inverse of projection x view_rotation */
+	float proj_view_rot[16];     /* projection x view_rotation */
+	float far_plane;
+	int32_t width, height;
+} vp_camera;
+VP_API int vp_world_render(vp_world *w, const vp_camera *cam, const uint32_t *mesh_queue, uint32_t n_mesh,
+			   const uint32_t *svl_queue, uint32_t n_svl, uint32_t *rgba, float *depth, uint64_t *stats);
+
 /* Kernel timing: with timing on, every rebuild records CUDA events around
  * its passes on the context stream; vp_world_kernel_ms waits for the stream
  * and returns the summed milliseconds since the last call of ms[0] the shell

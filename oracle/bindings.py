@@ -349,3 +349,51 @@ def perspective_view(*args, **kw):
     """A column-major view-projection matrix (voxplat_gb300.camera)."""
     from voxplat_gb300.camera import perspective_view as pv
     return pv(*args, **kw)
+
+
+# ---------------------------------------------------------------------------
+# software rasteriser (resources/splat.*.glsl, resources/mesh.*.glsl)
+
+class _VpoCamera(ctypes.Structure):
+    _fields_ = [("projection", ctypes.c_float * 16), ("view_rotation", ctypes.c_float * 16),
+                ("view_translation", ctypes.c_float * 16), ("view_projection", ctypes.c_float * 16),
+                ("inv_proj_view_rot", ctypes.c_float * 16), ("proj_view_rot", ctypes.c_float * 16),
+                ("far_plane", ctypes.c_float), ("width", ctypes.c_int), ("height", ctypes.c_int)]
+
+
+class Frame:
+    """A frame drawn by the oracle's rasteriser: packed (depth << 32 | RGBA8)."""
+
+    def __init__(self, cam):
+        self.cam = _VpoCamera()
+        for k in ("projection", "view_rotation", "view_translation", "view_projection", "inv_proj_view_rot",
+                  "proj_view_rot"):
+            getattr(self.cam, k)[:] = [float(x) for x in np.asarray(cam[k], np.float32)]
+        self.cam.far_plane, self.cam.width, self.cam.height = cam["far_plane"], cam["width"], cam["height"]
+        self.w, self.h = cam["width"], cam["height"]
+        self.words = np.zeros(self.w * self.h, np.uint64)
+        lib = vpo_lib()
+        lib.vpo_frame_clear.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        lib.vpo_draw_splats.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int,
+                                        ctypes.c_void_p]
+        lib.vpo_draw_mesh.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                      ctypes.c_void_p]
+        self.lib = lib
+        lib.vpo_frame_clear(_vp(self.words), self.w, self.h)
+
+    def splats(self, svl, lod):
+        svl = np.ascontiguousarray(svl, np.int16)
+        self.lib.vpo_draw_splats(ctypes.byref(self.cam), _vp(svl), len(svl) // 4, int(lod), _vp(self.words))
+
+    def mesh(self, vbo, ibo):
+        vbo = np.ascontiguousarray(vbo, np.int16)
+        ibo = np.ascontiguousarray(ibo, np.uint32)
+        self.lib.vpo_draw_mesh(ctypes.byref(self.cam), _vp(vbo), _vp(ibo), len(ibo) // 6, _vp(self.words))
+
+    @property
+    def rgba(self):
+        return (self.words & 0xFFFFFFFF).astype(np.uint32).reshape(self.h, self.w)
+
+    @property
+    def depth(self):
+        return (self.words >> 32).astype(np.uint32).view(np.float32).reshape(self.h, self.w)

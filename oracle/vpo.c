@@ -737,3 +737,235 @@ uint8_t vpo_raycast(vpo_world *w, const float *origin, const float *vector, uint
 	}
 	return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* Software rasteriser (resources/splat.*.glsl, resources/mesh.*.glsl) */
+/* ------------------------------------------------------------------ */
+
+/* row `row` of m (column-major) times v, summed left to right */
+static float mv_row(const float *m, int row, const float *v)
+{
+	return ((m[row] * v[0] + m[4 + row] * v[1]) + m[8 + row] * v[2]) + m[12 + row] * v[3];
+}
+
+static void mat_vec(const float *m, const float *v, float *out)
+{
+	for (int i = 0; i < 4; i++) out[i] = mv_row(m, i, v);
+}
+
+static float signf_(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
+
+static uint32_t to8(float c)
+{
+	c = fminf(fmaxf(c, 0.0f), 1.0f);
+	return (uint32_t)(c * 255.0f + 0.5f);
+}
+
+static uint32_t float_bits(float f)
+{
+	uint32_t u;
+	memcpy(&u, &f, 4);
+	return u;
+}
+
+static void frame_put(uint64_t *frame, int width, int px, int py, float depth, const float rgb[3])
+{
+	const uint32_t rgba = to8(rgb[0]) | (to8(rgb[1]) << 8) | (to8(rgb[2]) << 16) | (255u << 24);
+	const float d = depth < 0.0f ? 0.0f : depth;
+	const uint64_t v = ((uint64_t)float_bits(d) << 32) | rgba;
+	uint64_t *p = frame + (size_t)py * width + px;
+	if (v < *p) *p = v;
+}
+
+/* fog (pow(max(d - 256 / far, 0.0001), 0.5) as a square root) and mix */
+static void fog_mix(const float col[3], float depth, float far_plane, float out[3])
+{
+	const float fog_start = 256.0f / far_plane;
+	const float fog = sqrtf(fmaxf(depth - fog_start, 0.0001f));
+	const float fc[3] = {0.5f, 0.5f, 0.7f};
+	for (int i = 0; i < 3; i++) out[i] = col[i] * (1.0f - fog) + fc[i] * fog;
+}
+
+void vpo_frame_clear(uint64_t *frame, int width, int height)
+{
+	const float bg[3] = {0.5f, 0.5f, 0.7f};
+	const uint32_t rgba = to8(bg[0]) | (to8(bg[1]) << 8) | (to8(bg[2]) << 16) | (255u << 24);
+	const uint64_t v = ((uint64_t)float_bits(1.0f) << 32) | rgba;
+	for (size_t i = 0; i < (size_t)width * height; i++) frame[i] = v;
+}
+
+/* splat.vert.glsl:34-54 + point rasterisation + splat.frag.glsl:25-157 */
+void vpo_draw_splats(const vpo_camera *cam, const int16_t *svl, uint64_t n, int lod_level, uint64_t *frame)
+{
+	const float lod = (float)(1 << lod_level);
+	const float W = (float)cam->width, H = (float)cam->height;
+	const float llen = sqrtf(1.0f + 1.0f);
+	const float light[3] = {-1.0f / llen, 1.0f / llen, 0.0f / llen};
+	for (uint64_t k = 0; k < n; k++) {
+		const int16_t *sp = svl + 4 * k;
+		const float a[4] = {(float)sp[0] + 0.5f * lod, (float)sp[1] + 0.5f * lod, (float)sp[2] + 0.5f * lod, 1.0f};
+		float vv[4], clip[4];
+		mat_vec(cam->view_translation, a, vv);
+		mat_vec(cam->proj_view_rot, vv, clip);
+		if (!(clip[3] > 0.0f) || fabsf(clip[0]) > clip[3] || fabsf(clip[1]) > clip[3] || fabsf(clip[2]) > clip[3])
+			continue;
+		const float ratio = W / H;
+		const float reduce = fmaxf(fabsf(clip[0] * ratio / clip[3]), fabsf(clip[1] / clip[3])) + 0.03f;
+		const float size = (H * 1.1f) / clip[2] * fmaxf(reduce, 1.0f);
+		const float ps = fminf(fmaxf(size * lod, 1.0f), 64.0f);
+		const float xw = (clip[0] / clip[3] * 0.5f + 0.5f) * W, yw = (clip[1] / clip[3] * 0.5f + 0.5f) * H;
+		const int c = sp[3];
+		const float shadow = (float)((c >> 6) & 1);
+		const float f = fmaxf(0.7f, 1.0f - shadow);
+		const float vcol[3] = {(float)((c >> 4) & 3) / 3.0f * f, (float)((c >> 2) & 3) / 3.0f * f,
+				       (float)(c & 3) / 3.0f * f};
+		int x0 = (int)ceilf(xw - ps * 0.5f - 0.5f), x1 = (int)ceilf(xw + ps * 0.5f - 0.5f) - 1;
+		int y0 = (int)ceilf(yw - ps * 0.5f - 0.5f), y1 = (int)ceilf(yw + ps * 0.5f - 0.5f) - 1;
+		if (x0 < 0) x0 = 0;
+		if (y0 < 0) y0 = 0;
+		if (x1 > cam->width - 1) x1 = cam->width - 1;
+		if (y1 > cam->height - 1) y1 = cam->height - 1;
+		for (int py = y0; py <= y1; py++)
+			for (int px = x0; px <= x1; px++) {
+				const float rc[4] = {((float)px + 0.5f) / W * 2.0f - 1.0f, ((float)py + 0.5f) / H * 2.0f - 1.0f,
+						     -1.0f, 1.0f};
+				float r4[4];
+				mat_vec(cam->inv_proj_view_rot, rc, r4);
+				const float rv[3] = {r4[0] / r4[3], r4[1] / r4[3], r4[2] / r4[3]};
+				const float len = sqrtf((rv[0] * rv[0] + rv[1] * rv[1]) + rv[2] * rv[2]);
+				const float ray[3] = {rv[0] / len, rv[1] / len, rv[2] / len};
+				float tmin[3], tmax[3];
+				for (int i = 0; i < 3; i++) {
+					const float inv = 1.0f / ray[i];
+					const float tb = (vv[i] - 0.5f * lod) * inv, tt = (vv[i] + 0.5f * lod) * inv;
+					tmin[i] = fminf(tt, tb);
+					tmax[i] = fmaxf(tt, tb);
+				}
+				const float t0 = fmaxf(fmaxf(tmin[0], tmin[1]), fmaxf(tmin[0], tmin[2]));
+				const float t1 = fminf(fminf(tmax[0], tmax[1]), fminf(tmax[0], tmax[2]));
+				if (!(t0 <= t1)) continue;
+				const float depth = t0 / cam->far_plane;
+				if (!(depth < 1.0f)) continue;
+				float hit[3], habs[3];
+				for (int i = 0; i < 3; i++) {
+					hit[i] = vv[i] - ray[i] * t0;
+					habs[i] = fabsf(hit[i]);
+				}
+				const float md = fmaxf(fmaxf(habs[0], habs[1]), habs[2]);
+				float r[3];
+				for (int i = 0; i < 3; i++) r[i] = -((habs[i] == md ? 1.0f : 0.0f) * signf_(hit[i]));
+				const float s = signf_((r[0] * light[0] + r[1] * light[1]) + r[2] * light[2]);
+				const float g = fmaxf(fmaxf(0.7f, shadow), s);
+				const float col[3] = {vcol[0] * g, vcol[1] * g, vcol[2] * g};
+				float out[3];
+				fog_mix(col, depth, cam->far_plane, out);
+				frame_put(frame, cam->width, px, py, depth, out);
+			}
+	}
+}
+
+typedef struct {
+	float xw, yw, w;       /* window position, clip w */
+	float depth, col[3], uv[2], nrm[3];
+	int diamond;
+} mesh_vert;
+
+static void mesh_vertex(const vpo_camera *cam, const int16_t *v, mesh_vert *o, int *ok)
+{
+	static const float nlut[6][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, 0, 0}, {0, -1, 0}, {0, 0, -1}};
+	static const float ulut[4][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}};
+	const float a[4] = {(float)v[0], (float)v[1], (float)v[2], 1.0f};
+	float clip[4], vt[4];
+	mat_vec(cam->view_projection, a, clip);
+	mat_vec(cam->view_translation, a, vt);
+	*ok = clip[3] > 0.0f;
+	o->w = clip[3];
+	o->xw = (clip[0] / clip[3] * 0.5f + 0.5f) * (float)cam->width;
+	o->yw = (clip[1] / clip[3] * 0.5f + 0.5f) * (float)cam->height;
+	const float d = sqrtf(((vt[0] * vt[0] + vt[1] * vt[1]) + vt[2] * vt[2]) + vt[3] * vt[3]);
+	o->depth = d / cam->far_plane;
+	const float aow = 1.0f - fminf(d / 180.0f, 1.0f);
+	const int c = v[3];
+	const float shadow = (float)((c >> 13) & 1);
+	const float ao = fminf((float)((c >> 6) & 3), 2.0f) / 12.0f;
+	const float f = fmaxf(1.0f - shadow, 0.6f);
+	const float g = 1.0f - ao * aow;
+	o->col[0] = (float)((c >> 4) & 3) / 3.0f * f * g;
+	o->col[1] = (float)((c >> 2) & 3) / 3.0f * f * g;
+	o->col[2] = (float)(c & 3) / 3.0f * f * g;
+	const int ni = (c >> 8) & 7;
+	for (int i = 0; i < 3; i++) o->nrm[i] = ni < 6 ? nlut[ni][i] : 0.0f;
+	o->uv[0] = ulut[(c >> 11) & 3][0];
+	o->uv[1] = ulut[(c >> 11) & 3][1];
+	o->diamond = (c >> 14) & 3;
+}
+
+/* edge (a -> b) owns pixel centres exactly on it when it is a top or left
+ * edge of a counter-clockwise triangle (y up) */
+static int top_left(float ax, float ay, float bx, float by)
+{
+	const float dx = bx - ax, dy = by - ay;
+	return dy < 0.0f || (dy == 0.0f && dx < 0.0f);
+}
+
+static float edge_fn(float ax, float ay, float bx, float by, float px, float py)
+{
+	return (bx - ax) * (py - ay) - (by - ay) * (px - ax);
+}
+
+/* mesh.vert.glsl + back-face culling + triangle rasterisation with
+ * perspective-correct varyings + mesh.frag.glsl */
+void vpo_draw_mesh(const vpo_camera *cam, const int16_t *vbo, const uint32_t *ibo, uint64_t nfaces, uint64_t *frame)
+{
+	for (uint64_t t = 0; t < 2 * nfaces; t++) {
+		mesh_vert v[3];
+		int ok = 1;
+		for (int k = 0; k < 3; k++) {
+			int okk;
+			mesh_vertex(cam, vbo + 4 * (size_t)ibo[3 * t + k], &v[k], &okk);
+			ok &= okk;
+		}
+		if (!ok) continue; /* a vertex behind the eye: the triangle is dropped */
+		const float area = edge_fn(v[0].xw, v[0].yw, v[1].xw, v[1].yw, v[2].xw, v[2].yw);
+		if (!(area > 0.0f)) continue; /* back-facing (GL_BACK, CCW front) or degenerate */
+		float mnx = fminf(fminf(v[0].xw, v[1].xw), v[2].xw), mxx = fmaxf(fmaxf(v[0].xw, v[1].xw), v[2].xw);
+		float mny = fminf(fminf(v[0].yw, v[1].yw), v[2].yw), mxy = fmaxf(fmaxf(v[0].yw, v[1].yw), v[2].yw);
+		int x0 = (int)fmaxf(floorf(mnx), 0.0f), x1 = (int)fminf(ceilf(mxx), (float)(cam->width - 1));
+		int y0 = (int)fmaxf(floorf(mny), 0.0f), y1 = (int)fminf(ceilf(mxy), (float)(cam->height - 1));
+		const int tl0 = top_left(v[1].xw, v[1].yw, v[2].xw, v[2].yw);
+		const int tl1 = top_left(v[2].xw, v[2].yw, v[0].xw, v[0].yw);
+		const int tl2 = top_left(v[0].xw, v[0].yw, v[1].xw, v[1].yw);
+		for (int py = y0; py <= y1; py++)
+			for (int px = x0; px <= x1; px++) {
+				const float fx = (float)px + 0.5f, fy = (float)py + 0.5f;
+				const float e0 = edge_fn(v[1].xw, v[1].yw, v[2].xw, v[2].yw, fx, fy);
+				const float e1 = edge_fn(v[2].xw, v[2].yw, v[0].xw, v[0].yw, fx, fy);
+				const float e2 = edge_fn(v[0].xw, v[0].yw, v[1].xw, v[1].yw, fx, fy);
+				if (!(e0 > 0.0f || (e0 == 0.0f && tl0)) || !(e1 > 0.0f || (e1 == 0.0f && tl1)) ||
+				    !(e2 > 0.0f || (e2 == 0.0f && tl2)))
+					continue;
+				const float q0 = e0 / area / v[0].w, q1 = e1 / area / v[1].w, q2 = e2 / area / v[2].w;
+				const float qs = (q0 + q1) + q2;
+				const float b0 = q0 / qs, b1 = q1 / qs, b2 = q2 / qs;
+#define INTERP(f) ((b0 * v[0].f + b1 * v[1].f) + b2 * v[2].f)
+				const float depth = INTERP(depth);
+				if (!(depth < 1.0f)) continue;
+				float col[3], uv[2], nrm[3];
+				for (int i = 0; i < 3; i++) {
+					col[i] = INTERP(col[i]);
+					nrm[i] = INTERP(nrm[i]);
+				}
+				uv[0] = INTERP(uv[0]);
+				uv[1] = INTERP(uv[1]);
+#undef INTERP
+				float c2[3] = {col[0], col[1], col[2]};
+				if (!((v[2].diamond >> (uv[0] < uv[1] ? 1 : 0)) & 1))
+					for (int i = 0; i < 3; i++) c2[i] = col[i] * 0.6f;
+				if (nrm[1] < -0.9f || nrm[0] > 0.9f)
+					for (int i = 0; i < 3; i++) c2[i] = col[i] * 0.6f;
+				float out[3];
+				fog_mix(c2, depth, cam->far_plane, out);
+				frame_put(frame, cam->width, px, py, depth, out);
+			}
+	}
+}

@@ -110,6 +110,26 @@ uint64_t vpo_octree_cull(int root_bitw, const int max_bitw[3], const float *plan
  * first solid voxel along the ray (0 if none within 4095 steps), its
  * coordinates and the normal of the face entered (normal zeroed first). */
 uint8_t vpo_raycast(vpo_world *w, const float *origin, const float *vector, uint32_t *coord, int8_t *normal);
+/* Software rasteriser of the splat and mesh shaders (resources/splat.vert.glsl,
+ * splat.frag.glsl, mesh.vert.glsl, mesh.frag.glsl), the semantics the CUDA
+ * rasteriser implements. Matrices are column-major float[16]. The frame is
+ * width x height packed words, (depth bits << 32) | RGBA8, initialised by
+ * vpo_frame_clear; a fragment keeps the minimum (GL_LESS; equal depths keep
+ * the smaller colour word). */
+typedef struct vpo_camera {
+	float projection[16], view_rotation[16], view_translation[16];
+	float view_projection[16];   /* projection x view_rotation x view_translation */
+	float inv_proj_view_rot[16]; /* inverse of projection x view_rotation */
+	float proj_view_rot[16];     /* projection x view_rotation */
+	float far_plane;
+	int width, height;
+} vpo_camera;
+void vpo_frame_clear(uint64_t *frame, int width, int height);
+/* n splats (4 int16 each) drawn with u_lod = 2^lod */
+void vpo_draw_splats(const vpo_camera *cam, const int16_t *svl, uint64_t n, int lod, uint64_t *frame);
+/* nfaces quads: 16 int16 of vertices and 6 u32 indices (relative to the
+ * chunk's vertices) per face */
+void vpo_draw_mesh(const vpo_camera *cam, const int16_t *vbo, const uint32_t *ibo, uint64_t nfaces, uint64_t *frame);
 /* make_mesh per chunk: distance from the chunk centre to origin < 512. */
 void vpo_mesh_flags(int root_bitw, const int max_bitw[3], const float *origin, uint8_t *make_mesh);
 uint64_t vpo_rebuild(vpo_world *w, const uint32_t *chunks, uint32_t n, const uint8_t *make_mesh, int lod_max,

@@ -9,8 +9,10 @@
 #include "vp_gen.h"
 #include "vp_cull.h"
 #include "vp_raycast.h"
+#include "vp_render.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -237,6 +239,8 @@ VP_API void vp_world_destroy(vp_world *w)
 	dev_free(w->d_flags);
 	dev_free(w->d_runidx);
 	dev_free(w->d_rays);
+	dev_free(w->d_render);
+	dev_free(w->d_frame);
 	dev_free(w->d_set);
 	dev_free(w->d_items);
 	dev_free(w->d_outs);
@@ -871,6 +875,106 @@ VP_API int vp_world_raycast(vp_world *w, uint32_t n, const float *origins, const
 	CK(cudaMemcpyAsync(normals, d_n, 3u * n, cudaMemcpyDeviceToHost, st));
 	CK(cudaStreamSynchronize(st));
 	return VP_OK;
+}
+
+static_assert(sizeof(vp_camera) == sizeof(RenderCam), "camera layout");
+
+static size_t a256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+VP_API int vp_world_render(vp_world *w, const vp_camera *cam, const uint32_t *mesh_queue, uint32_t n_mesh,
+			   const uint32_t *svl_queue, uint32_t n_svl, uint32_t *rgba, float *depth, uint64_t *stats)
+{
+	if (!w || !cam || !rgba || cam->width <= 0 || cam->height <= 0) return VP_EINVAL;
+	const uint64_t npx = (uint64_t)cam->width * (uint64_t)cam->height;
+	if (npx > (1ull << 26) || !(cam->far_plane > 0.0f)) return VP_EINVAL;
+	if ((n_mesh && !mesh_queue) || (n_svl && !svl_queue)) return VP_EINVAL;
+	for (uint32_t i = 0; i < n_mesh; i++)
+		if (mesh_queue[i] >= w->nchunks) return VP_EINVAL;
+	for (uint32_t i = 0; i < n_svl; i++) {
+		const uint32_t l = svl_queue[i] >> 24, node = svl_queue[i] & 0xFFFFFFu;
+		if ((int)l > w->grouped_lod || node >= w->nchunks) return VP_EINVAL;
+	}
+	CK(cudaSetDevice(w->ctx->device));
+	cudaStream_t st = w->ctx->stream;
+	int rc;
+	/* scratch: queues, segments + first splat, meshes + first triangle, totals */
+	const size_t o_sq = 0, o_mq = a256(o_sq + 4u * (size_t)n_svl);
+	const size_t o_seg = a256(o_mq + 4u * (size_t)n_mesh);
+	const size_t o_sf = a256(o_seg + sizeof(RenderSeg) * n_svl);
+	const size_t o_me = a256(o_sf + 8u * (size_t)n_svl);
+	const size_t o_mf = a256(o_me + sizeof(RenderMesh) * n_mesh);
+	const size_t o_tot = a256(o_mf + 8u * (size_t)n_mesh);
+	const size_t o_bc = a256(o_tot + 16u);
+	const size_t prep_bytes = a256(o_bc + 8u);
+	if (w->render_cap < prep_bytes) {
+		dev_free(w->d_render);
+		w->render_cap = 0;
+		if ((rc = dev_alloc(&w->d_render, prep_bytes))) return rc;
+		w->render_cap = prep_bytes;
+	}
+	uint8_t *R = w->d_render;
+	if (n_svl) CK(cudaMemcpyAsync(R + o_sq, svl_queue, 4u * (size_t)n_svl, cudaMemcpyHostToDevice, st));
+	if (n_mesh) CK(cudaMemcpyAsync(R + o_mq, mesh_queue, 4u * (size_t)n_mesh, cudaMemcpyHostToDevice, st));
+	uint64_t *tot = (uint64_t *)(R + o_tot);
+	CK(cudaMemsetAsync(tot, 0, 16, st));
+	cudaError_t e = launch_render_prep((const uint32_t *)(R + o_sq), n_svl, w->d_node_off, w->d_node_items,
+					   w->nchunks, (const uint32_t *)(R + o_mq), n_mesh, w->d_outs,
+					   (RenderSeg *)(R + o_seg), (uint64_t *)(R + o_sf), (RenderMesh *)(R + o_me),
+					   (uint64_t *)(R + o_mf), tot, st);
+	if (e != cudaSuccess) return cuda_fail(e, "render prep");
+	uint64_t totals[2];
+	CK(cudaMemcpyAsync(totals, tot, 16, cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	/* frame words, RGBA, depth, and the two lists of large footprints */
+	const uint32_t big_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(totals[0] + totals[1], 1), 4u << 20);
+	const size_t f_rgba = a256(8u * npx), f_depth = a256(f_rgba + 4u * npx), f_big = a256(f_depth + 4u * npx);
+	const size_t frame_bytes = a256(f_big + 16u * (size_t)big_cap);
+	if (w->frame_cap < frame_bytes) {
+		dev_free(w->d_frame);
+		w->frame_cap = 0;
+		if ((rc = dev_alloc(&w->d_frame, frame_bytes))) return rc;
+		w->frame_cap = frame_bytes;
+	}
+	RenderArgs a;
+	memset(&a, 0, sizeof(a));
+	memcpy(&a.cam, cam, sizeof(a.cam));
+	const float llen = sqrtf(1.0f + 1.0f);
+	a.light[0] = -1.0f / llen;
+	a.light[1] = 1.0f / llen;
+	a.light[2] = 0.0f / llen;
+	a.splats = w->d_garena;
+	a.segs = (const RenderSeg *)(R + o_seg);
+	a.seg_first = (const uint64_t *)(R + o_sf);
+	a.nseg = n_svl;
+	a.nsplats = totals[0];
+	a.vbo = (const int16_t *)w->d_arena[1];
+	a.ibo = (const uint32_t *)w->d_arena[2];
+	a.meshes = (const RenderMesh *)(R + o_me);
+	a.mesh_first = (const uint64_t *)(R + o_mf);
+	a.nmesh = n_mesh;
+	a.ntris = totals[1];
+	a.frame = (unsigned long long *)w->d_frame;
+	a.big = (uint64_t *)(w->d_frame + f_big);
+	a.big_count = (uint32_t *)(R + o_bc);
+	a.big_cap = big_cap;
+	if (n_svl && !a.splats) return VP_EINVAL;
+	uint32_t *d_rgba = (uint32_t *)(w->d_frame + f_rgba);
+	float *d_depth = (float *)(w->d_frame + f_depth);
+	e = launch_render(a, d_rgba, depth ? d_depth : nullptr, w->ctx->sm_count, st);
+	if (e != cudaSuccess) return cuda_fail(e, "render");
+	w->launches += 7;
+	uint32_t big[2];
+	CK(cudaMemcpyAsync(rgba, d_rgba, 4u * npx, cudaMemcpyDeviceToHost, st));
+	if (depth) CK(cudaMemcpyAsync(depth, d_depth, 4u * npx, cudaMemcpyDeviceToHost, st));
+	CK(cudaMemcpyAsync(big, a.big_count, 8, cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	if (stats) {
+		stats[0] = totals[0];
+		stats[1] = totals[1];
+		stats[2] = big[0];
+		stats[3] = big[1];
+	}
+	return (big[0] > big_cap || big[1] > big_cap) ? VP_EOVERFLOW : VP_OK;
 }
 
 VP_API int vp_world_results(vp_world *w, vp_chunk_result *out, uint32_t n)

@@ -74,6 +74,11 @@ struct vp_world {
 	uint64_t runidx_cap = 0;
 	uint8_t *d_rays = nullptr;
 	size_t rays_cap = 0;
+	/* rasteriser */
+	uint8_t *d_render = nullptr;            /* queues, segments, scans, big lists */
+	size_t render_cap = 0;
+	uint8_t *d_frame = nullptr;             /* frame words, RGBA, depth */
+	size_t frame_cap = 0;
 	uint32_t shadow_w = 0;
 	uint64_t *d_shell_bits = nullptr;
 	uint8_t *d_shell_col = nullptr;

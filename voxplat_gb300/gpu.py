@@ -58,6 +58,22 @@ class BatchTune(ctypes.Structure):
                 "ms": round(float(self.ms), 4)}
 
 
+class Camera(ctypes.Structure):
+    _fields_ = [("projection", ctypes.c_float * 16), ("view_rotation", ctypes.c_float * 16),
+                ("view_translation", ctypes.c_float * 16), ("view_projection", ctypes.c_float * 16),
+                ("inv_proj_view_rot", ctypes.c_float * 16), ("proj_view_rot", ctypes.c_float * 16),
+                ("far_plane", ctypes.c_float), ("width", ctypes.c_int32), ("height", ctypes.c_int32)]
+
+    @classmethod
+    def from_dict(cls, d):
+        c = cls()
+        for k in ("projection", "view_rotation", "view_translation", "view_projection", "inv_proj_view_rot",
+                  "proj_view_rot"):
+            getattr(c, k)[:] = [float(x) for x in np.asarray(d[k], np.float32)]
+        c.far_plane, c.width, c.height = d["far_plane"], d["width"], d["height"]
+        return c
+
+
 class ServeStats(ctypes.Structure):
     _fields_ = [("batches", ctypes.c_uint32), ("edits", ctypes.c_uint32), ("max_batch", ctypes.c_uint32),
                 ("deferred", ctypes.c_uint32), ("chunks_remeshed", ctypes.c_uint64), ("busy_s", ctypes.c_double),
@@ -119,6 +135,7 @@ def load(build_if_missing=True):
         "vp_world_camera_modes": (I, [V, V, V]),
         "vp_world_raycast": (I, [V, U32, V, V, V, V, V]),
         "vp_world_save": (I, [V, ctypes.c_char_p]),
+        "vp_world_render": (I, [V, V, V, U32, V, U32, V, V, V]),
         "vp_world_open": (I, [V, ctypes.c_char_p, PV]),
         "vp_world_read_svl": (I, [V, U64, U64, V]),
         "vp_world_read_vbo": (I, [V, U64, U64, V]),
@@ -331,6 +348,19 @@ class DeviceWorld:
         check(self.lib.vp_world_cull(self.h, _p(vp), _p(org), top_lod, _p(mq), len(mq), ctypes.byref(nm), _p(sq),
                                      len(sq), ctypes.byref(ns)), "vp_world_cull")
         return mq[:nm.value].copy(), sq[:ns.value].copy()
+
+    def render(self, cam, mesh_queue, svl_queue):
+        """(rgba[h, w] uint32, depth[h, w] float32, stats[4]) of the drawn
+        queues; cam is a voxplat_gb300.camera.camera() dict."""
+        c = Camera.from_dict(cam)
+        mq = np.ascontiguousarray(mesh_queue, np.uint32)
+        sq = np.ascontiguousarray(svl_queue, np.uint32)
+        rgba = np.zeros((cam["height"], cam["width"]), np.uint32)
+        depth = np.zeros((cam["height"], cam["width"]), np.float32)
+        stats = np.zeros(4, np.uint64)
+        check(self.lib.vp_world_render(self.h, ctypes.byref(c), _p(mq), len(mq), _p(sq), len(sq), _p(rgba),
+                                       _p(depth), _p(stats)), "vp_world_render")
+        return rgba, depth, stats
 
     def save(self, path):
         """Write the world (streams + shadow map) in the VPW1 file format."""
