@@ -307,6 +307,9 @@ def run_ours(args):
     if rank == 0:
         out["clocks"] = clk.summary()
         out["picking"] = picking(dw)
+        dw.rebuild(LOD_MAX, group=True)
+        dw.finish()
+        out["render"] = render_frame(dw, CAMERA)
         dw.close()
         if not args.skip_edits:
             out["edit_serving"] = edit_serving(ctx)
@@ -475,6 +478,23 @@ def draw_cull(dw, reps=20):
     nodes = sum((dw.nchunks >> (3 * l)) for l in range(5))
     return {"ms_per_cull": round(ms, 3), "octree_nodes": int(nodes), "mesh_queue": int(len(mq)),
             "splat_queue": int(len(sq)), "ms_per_camera_modes": round(mm, 3)}
+
+
+def render_frame(dw, modes_eye, width=1920, height=1080, reps=5):
+    """Draw cull + CUDA rasteriser of the splat and mesh shaders at 1080p
+    from the bench camera, through the C ABI (frame back to host)."""
+    from voxplat_gb300.camera import camera
+    eye = np.asarray(modes_eye, np.float32)
+    cam = camera(eye, eye + np.array([0.6, -0.25, 1.0]), width, height, fov_deg=70.0, far=4096.0)
+    mq, sq = dw.cull(cam["view_projection"], eye)
+    rgba, depth, stats = dw.render(cam, mq, sq)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        rgba, depth, stats = dw.render(cam, mq, sq)
+    ms = (time.perf_counter() - t0) / reps * 1e3
+    return {"width": width, "height": height, "ms_per_frame": round(ms, 3), "splats": int(stats[0]),
+            "triangles": int(stats[1]), "pixels_drawn": int((depth < 1.0).sum()),
+            "splats_per_s": round(stats[0] / (ms / 1e3), 1), "mesh_chunks": int(len(mq)), "splat_nodes": int(len(sq))}
 
 
 def picking(dw, n=65536, seed=6):
