@@ -115,6 +115,16 @@ VP_API int vp_world_rebuild(vp_world *w, int lod_max, unsigned flags);
 VP_API int vp_world_finish(vp_world *w);
 
 VP_API int vp_world_results(vp_world *w, vp_chunk_result *out, uint32_t n);
+/* A full rebuild whose outputs stream into host buffers while the GPU
+ * works (pinned buffers): the geometry pass runs as `slabs` launches (1..16)
+ * over interleaved parts of the work order, and each part's output ranges
+ * are copied back on a second stream while the next part computes; then the
+ * result records. Same outputs and layout as vp_world_rebuild +
+ * vp_world_finish + vp_world_results + vp_world_read_outputs, which it falls
+ * back to when an arena has to grow. */
+VP_API int vp_world_rebuild_to_host(vp_world *w, int lod_max, unsigned flags, int slabs, void *svl,
+				    uint64_t svl_bytes, void *vbo, uint64_t vbo_bytes, void *ibo, uint64_t ibo_bytes,
+				    vp_chunk_result *results, uint64_t used_bytes[3]);
 /* Copy the used part of the three output arenas (splats, vertices,
  * indices) into host buffers, with the arena layout the results' offsets
  * index (a NULL buffer is skipped). used_bytes[] gets each used size;

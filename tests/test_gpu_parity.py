@@ -174,3 +174,41 @@ def test_read_outputs_returns_the_arena_layout(ctx):
     assert used[0] >= int(np.max(res["svl_off"] + res["svl_total"])) * 2
     with pytest.raises(gpu.VoxGpuError):
         dw.read_outputs(svl[:16], vbo, ibo)
+
+
+@pytest.mark.parametrize("slabs", [1, 3, 8])
+def test_streamed_rebuild_matches_the_plain_sequence(ctx, slabs):
+    """vp_world_rebuild_to_host: the same records and output bytes as
+    rebuild + finish + results + read_outputs, also when the arenas start
+    too small (the streamed pass falls back and grows them)."""
+    w = worlds.cave_world(5, (2, 1, 2), seed=23)
+    modes = (np.arange(w.nchunks) % 3 == 0).astype(np.uint8)
+    ref = gpu.DeviceWorld(ctx, w)
+    ref.set_modes(modes)
+    ref.rebuild(lod_max=4, group=True)
+    ref.finish()
+    res_a = ref.results()
+    bufs_a = [np.zeros(1 << 23, np.int16), np.zeros(1 << 23, np.int16), np.zeros(1 << 22, np.uint32)]
+    used_a = ref.read_outputs(*bufs_a)
+    for tiny in (False, True):
+        dw = gpu.DeviceWorld(ctx, w)
+        dw.set_modes(modes)
+        if tiny:
+            dw.reserve(16, 16, 16)
+        res_b = np.zeros(w.nchunks, gpu.RESULT_DTYPE)
+        bufs_b = [np.zeros(1 << 23, np.int16), np.zeros(1 << 23, np.int16), np.zeros(1 << 22, np.uint32)]
+        used_b = dw.rebuild_to_host(4, *bufs_b, res_b, group=True, slabs=slabs)
+        # offsets differ (the slabs allocate in another order): compare per chunk
+        assert (res_b["status"] == 0).all()
+        for c in range(w.nchunks):
+            ra, rb = res_a[c], res_b[c]
+            assert np.array_equal(ra["svl_items"], rb["svl_items"]) and ra["vbo_items"] == rb["vbo_items"]
+            for arr_a, arr_b, ko, kn in ((bufs_a[0], bufs_b[0], "svl_off", "svl_total"),
+                                         (bufs_a[1], bufs_b[1], "vbo_off", "vbo_items"),
+                                         (bufs_a[2], bufs_b[2], "ibo_off", "ibo_items")):
+                n = int(ra[kn])
+                assert np.array_equal(arr_a[int(ra[ko]):int(ra[ko]) + n], arr_b[int(rb[ko]):int(rb[ko]) + n]), (c, kn)
+        assert sum(used_b) >= sum(int(res_b[k].astype(np.int64).sum()) for k in ("svl_total",)) * 2
+        off, items = dw.group_nodes(0)
+        offr, itemsr = ref.group_nodes(0)
+        assert np.array_equal(items, itemsr)

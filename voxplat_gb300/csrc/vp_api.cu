@@ -241,6 +241,15 @@ VP_API void vp_world_destroy(vp_world *w)
 	dev_free(w->d_rays);
 	dev_free(w->d_render);
 	dev_free(w->d_frame);
+	dev_free(w->d_stream_items);
+	dev_free(w->d_slab_q);
+	if (w->copy_stream) {
+		cudaStreamSynchronize(w->copy_stream);
+		cudaStreamDestroy(w->copy_stream);
+	}
+	for (int k = 0; k < kMaxStreamSlabs; k++)
+		if (w->slab_ev[k]) cudaEventDestroy(w->slab_ev[k]);
+	if (w->h_snap) cudaFreeHost(w->h_snap);
 	dev_free(w->d_set);
 	dev_free(w->d_items);
 	dev_free(w->d_outs);
@@ -517,7 +526,9 @@ static int ensure_items(vp_world *w)
 	CK(cudaMemcpyAsync(w->d_items, it.data(), it.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
 			   w->ctx->stream));
 	CK(cudaStreamSynchronize(w->ctx->stream));
+	w->h_items.swap(it);
 	w->items_dirty = false;
+	w->stream_slabs = 0; /* the slab orders follow the work order */
 	return VP_OK;
 }
 
@@ -975,6 +986,121 @@ VP_API int vp_world_render(vp_world *w, const vp_camera *cam, const uint32_t *me
 		stats[3] = big[1];
 	}
 	return (big[0] > big_cap || big[1] > big_cap) ? VP_EOVERFLOW : VP_OK;
+}
+
+VP_API int vp_world_rebuild_to_host(vp_world *w, int lod_max, unsigned flags, int slabs, void *svl,
+				    uint64_t svl_bytes, void *vbo, uint64_t vbo_bytes, void *ibo, uint64_t ibo_bytes,
+				    vp_chunk_result *results, uint64_t used_bytes[3])
+{
+	if (!w || !w->uploaded || !results || !used_bytes) return VP_EINVAL;
+	if (lod_max < 0 || lod_max >= VP_MAX_LEVELS || slabs < 1 || slabs > kMaxStreamSlabs) return VP_EINVAL;
+	if ((flags & VP_REBUILD_PLAIN) || w->root_bitw == 7) {
+		/* per-chunk launches and 128^3 chunks take the plain sequence */
+		int rc;
+		if ((rc = vp_world_rebuild(w, lod_max, flags)) || (rc = vp_world_finish(w)) ||
+		    (rc = vp_world_results(w, results, w->nchunks)))
+			return rc;
+		return vp_world_read_outputs(w, svl, svl_bytes, vbo, vbo_bytes, ibo, ibo_bytes, used_bytes);
+	}
+	CK(cudaSetDevice(w->ctx->device));
+	vp_ctx *ctx = w->ctx;
+	cudaStream_t st = ctx->stream;
+	int rc;
+	if ((rc = ensure_items(w)) || (rc = vpi_ensure_arenas(w))) return rc;
+	if (!w->copy_stream) {
+		CK(cudaStreamCreateWithFlags(&w->copy_stream, cudaStreamNonBlocking));
+		for (int k = 0; k < kMaxStreamSlabs; k++) CK(cudaEventCreateWithFlags(&w->slab_ev[k], cudaEventDisableTiming));
+		CK(cudaHostAlloc((void **)&w->h_snap, 3u * kMaxStreamSlabs * sizeof(unsigned long long), cudaHostAllocDefault));
+		if ((rc = dev_alloc(&w->d_slab_q, kMaxStreamSlabs)) || (rc = dev_alloc(&w->d_stream_items, w->nchunks)))
+			return rc;
+	}
+	/* slab k takes ranks k, k + S, k + 2S, ... of the longest-first order, so
+	 * every slab holds a similar mix and is itself longest first */
+	std::vector<uint32_t> first(slabs + 1, 0);
+	if (w->stream_slabs != slabs) {
+		std::vector<WorkItem> order;
+		order.reserve(w->nchunks);
+		for (int k = 0; k < slabs; k++)
+			for (uint32_t i = (uint32_t)k; i < w->nchunks; i += (uint32_t)slabs) order.push_back(w->h_items[i]);
+		CK(cudaMemcpyAsync(w->d_stream_items, order.data(), order.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
+				   st));
+		CK(cudaStreamSynchronize(st));
+		w->stream_slabs = slabs;
+	}
+	for (int k = 0; k < slabs; k++) first[k + 1] = first[k] + (w->nchunks - (uint32_t)k + (uint32_t)slabs - 1) / slabs;
+	CK(cudaMemsetAsync(w->d_cursors, 0, 3 * sizeof(unsigned long long), st));
+	CK(cudaMemsetAsync(w->d_slab_q, 0, kMaxStreamSlabs * sizeof(unsigned int), st));
+	GeoLaunch L;
+	memset(&L, 0, sizeof(L));
+	L.big_scratch = w->d_big;
+	L.big_slots = w->big_slots;
+	L.sets = w->d_set;
+	L.shell_items = w->d_items;
+	L.n_shell = w->nchunks;
+	L.threads = 512;
+	L.outs = w->d_outs;
+	L.lod_max = lod_max;
+	Arena *ar[3] = {&L.svl, &L.vbo, &L.ibo};
+	for (int a = 0; a < 3; a++) {
+		ar[a]->base = w->d_arena[a];
+		ar[a]->cap_units = w->cap[a];
+		ar[a]->cursor = w->d_cursors + a;
+	}
+	const int per_sm = geometry_ctas_per_sm(w->root_bitw, (int)L.threads);
+	L.ctas = (uint32_t)(ctx->sm_count * std::max(per_sm, 1));
+	GeoLaunch Ls = L;
+	Ls.run_shell = 1;
+	cudaError_t e = launch_geometry(w->root_bitw, Ls, st);
+	if (e != cudaSuccess) return cuda_fail(e, "shell launch");
+	for (int k = 0; k < slabs; k++) {
+		GeoLaunch Lg = L;
+		Lg.items = w->d_stream_items + first[k];
+		Lg.n_items = first[k + 1] - first[k];
+		Lg.queue = w->d_slab_q + k;
+		e = launch_geometry(w->root_bitw, Lg, st);
+		if (e != cudaSuccess) return cuda_fail(e, "geometry launch");
+		CK(cudaMemcpyAsync(w->h_snap + 3 * k, w->d_cursors, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+				   st));
+		CK(cudaEventRecord(w->slab_ev[k], st));
+	}
+	w->launches += 1 + slabs;
+	w->grouped_lod = -1;
+	if ((flags & VP_REBUILD_GROUP) && (rc = enqueue_group(w, lod_max))) return rc;
+	w->last_lod = lod_max;
+	w->last_flags = flags;
+	/* each slab's new output ranges go back while the next slab computes */
+	void *dst[3] = {svl, vbo, ibo};
+	const uint64_t cap_b[3] = {svl_bytes, vbo_bytes, ibo_bytes};
+	uint64_t prev[3] = {0, 0, 0};
+	bool overflow = false, short_buf = false;
+	for (int k = 0; k < slabs; k++) {
+		CK(cudaEventSynchronize(w->slab_ev[k]));
+		for (int a = 0; a < 3; a++) {
+			const uint64_t cur = w->h_snap[3 * k + a];
+			if (cur > w->cap[a]) overflow = true;
+			if (overflow || cur <= prev[a]) continue;
+			if (!dst[a] || cur * 16u > cap_b[a]) {
+				short_buf = short_buf || (cur * 16u > cap_b[a] && dst[a]);
+				prev[a] = cur;
+				continue;
+			}
+			CK(cudaMemcpyAsync((uint8_t *)dst[a] + prev[a] * 16u, (const uint8_t *)w->d_arena[a] + prev[a] * 16u,
+					   (cur - prev[a]) * 16u, cudaMemcpyDeviceToHost, w->copy_stream));
+			prev[a] = cur;
+		}
+	}
+	if (overflow) {
+		/* an arena was too small: grow it and run the plain sequence */
+		CK(cudaStreamSynchronize(w->copy_stream));
+		if ((rc = vp_world_finish(w)) || (rc = vp_world_results(w, results, w->nchunks))) return rc;
+		return vp_world_read_outputs(w, svl, svl_bytes, vbo, vbo_bytes, ibo, ibo_bytes, used_bytes);
+	}
+	CK(cudaMemcpyAsync(results, w->d_outs, (size_t)w->nchunks * sizeof(ChunkOut), cudaMemcpyDeviceToHost,
+			   w->copy_stream));
+	CK(cudaStreamSynchronize(w->copy_stream));
+	CK(cudaStreamSynchronize(st));
+	for (int a = 0; a < 3; a++) used_bytes[a] = prev[a] * 16u;
+	return short_buf ? VP_EOVERFLOW : VP_OK;
 }
 
 VP_API int vp_world_results(vp_world *w, vp_chunk_result *out, uint32_t n)

@@ -48,6 +48,8 @@ struct vp_ctx {
 	uint64_t *d_scalars = nullptr; /* [0] cursor, [1] off, [2] len|status */
 };
 
+constexpr int kMaxStreamSlabs = 16;
+
 struct vp_world {
 	vp_ctx *ctx;
 	int root_bitw;
@@ -75,6 +77,14 @@ struct vp_world {
 	uint8_t *d_rays = nullptr;
 	size_t rays_cap = 0;
 	/* rasteriser */
+	/* streamed rebuilds: work order by slab, per-slab queues, copy stream */
+	std::vector<WorkItem> h_items;          /* longest-first work order */
+	WorkItem *d_stream_items = nullptr;
+	int stream_slabs = 0;
+	unsigned int *d_slab_q = nullptr;
+	cudaStream_t copy_stream = nullptr;
+	cudaEvent_t slab_ev[kMaxStreamSlabs] = {};
+	unsigned long long *h_snap = nullptr;   /* pinned: 3 cursors per slab */
 	uint8_t *d_render = nullptr;            /* queues, segments, scans, big lists */
 	size_t render_cap = 0;
 	uint8_t *d_frame = nullptr;             /* frame words, RGBA, depth */

@@ -131,6 +131,7 @@ def load(build_if_missing=True):
         "vp_world_reserve": (I, [V, V]),
         "vp_world_results": (I, [V, V, U32]),
         "vp_world_read_outputs": (I, [V, V, U64, V, U64, V, U64, V]),
+        "vp_world_rebuild_to_host": (I, [V, I, ctypes.c_uint, I, V, U64, V, U64, V, U64, V, V]),
         "vp_world_cull": (I, [V, V, V, I, V, U32, ctypes.POINTER(U32), V, U32, ctypes.POINTER(U32)]),
         "vp_world_camera_modes": (I, [V, V, V]),
         "vp_world_raycast": (I, [V, U32, V, V, V, V, V]),
@@ -328,6 +329,17 @@ class DeviceWorld:
         out = np.zeros(self.nchunks, RESULT_DTYPE)
         check(self.lib.vp_world_results(self.h, _p(out), self.nchunks), "vp_world_results")
         return out
+
+    def rebuild_to_host(self, lod_max, svl, vbo, ibo, results, group=False, slabs=4):
+        """A full rebuild streaming its outputs into the given host arrays
+        (pinned copies fastest) and the result records into `results`
+        (RESULT_DTYPE array); returns the used bytes of each output."""
+        used = np.zeros(3, np.uint64)
+        flags = VP_REBUILD_PERSISTENT | (VP_REBUILD_GROUP if group else 0)
+        check(self.lib.vp_world_rebuild_to_host(self.h, lod_max, flags, slabs, _p(svl), svl.nbytes, _p(vbo),
+                                                vbo.nbytes, _p(ibo), ibo.nbytes, _p(results), _p(used)),
+              "vp_world_rebuild_to_host")
+        return [int(u) for u in used]
 
     def read_outputs(self, svl, vbo, ibo):
         """Copy the used part of the three output arenas into the given
