@@ -212,3 +212,64 @@ def test_streamed_rebuild_matches_the_plain_sequence(ctx, slabs):
         off, items = dw.group_nodes(0)
         offr, itemsr = ref.group_nodes(0)
         assert np.array_equal(items, itemsr)
+
+
+def _same_outputs(res_a, bufs_a, res_b, bufs_b):
+    """Per-chunk comparison of two rebuilds' records and output bytes (the
+    allocation order, and so the offsets, may differ)."""
+    for c in range(len(res_a)):
+        ra, rb = res_a[c], res_b[c]
+        if not (np.array_equal(ra["svl_items"], rb["svl_items"]) and ra["vbo_items"] == rb["vbo_items"]
+                and ra["ibo_items"] == rb["ibo_items"] and rb["status"] == 0):
+            return c
+        for arr_a, arr_b, ko, kn in ((bufs_a[0], bufs_b[0], "svl_off", "svl_total"),
+                                     (bufs_a[1], bufs_b[1], "vbo_off", "vbo_items"),
+                                     (bufs_a[2], bufs_b[2], "ibo_off", "ibo_items")):
+            n = int(ra[kn])
+            if not np.array_equal(arr_a[int(ra[ko]):int(ra[ko]) + n], arr_b[int(rb[ko]):int(rb[ko]) + n]):
+                return c
+    return None
+
+
+@pytest.mark.parametrize("tiny", [False, True])
+def test_pipelined_rebuilds_match_the_synchronous_one(ctx, tiny):
+    """vp_world_rebuild_to_host_async over alternating host buffer sets:
+    every call's outputs equal a synchronous rebuild's at the same LOD, the
+    records of call k final once call k+1 (or outputs_wait) returned; with
+    arenas that start too small the first call grows them and reruns."""
+    w = worlds.cave_world(5, (2, 1, 2), seed=29)
+    modes = (np.arange(w.nchunks) % 4 == 1).astype(np.uint8)
+    lods = [4, 2, 3, 4, 1, 3]
+    ref = gpu.DeviceWorld(ctx, w)
+    ref.set_modes(modes)
+    want = {}
+    for lod in set(lods):
+        res = np.zeros(w.nchunks, gpu.RESULT_DTYPE)
+        bufs = [np.zeros(1 << 22, np.int16), np.zeros(1 << 22, np.int16), np.zeros(1 << 21, np.uint32)]
+        ref.rebuild_to_host(lod, *bufs, res, slabs=3)
+        want[lod] = (res, bufs)
+    dw = gpu.DeviceWorld(ctx, w)
+    dw.set_modes(modes)
+    if tiny:
+        dw.reserve(16, 16, 16)
+    sets = [([np.zeros(1 << 22, np.int16), np.zeros(1 << 22, np.int16), np.zeros(1 << 21, np.uint32)],
+             np.zeros(w.nchunks, gpu.RESULT_DTYPE)) for _ in range(2)]
+    for k, lod in enumerate(lods):
+        bufs, res = sets[k % 2]
+        for b in bufs:
+            b.fill(0)
+        res.fill(0)
+        used = dw.rebuild_to_host_async(lod, *bufs, res, slabs=4)
+        assert all(u <= b.nbytes for u, b in zip(used, bufs))
+        if k >= 1:
+            pbufs, pres = sets[(k - 1) % 2]  # call k-1's outputs are final now
+            assert _same_outputs(want[lods[k - 1]][0], want[lods[k - 1]][1], pres, pbufs) is None, k - 1
+    dw.outputs_wait()
+    k = len(lods) - 1
+    bufs, res = sets[k % 2]
+    assert _same_outputs(want[lods[k]][0], want[lods[k]][1], res, bufs) is None, k
+    # a synchronous rebuild after pipelined ones sees the whole arenas again
+    res = np.zeros(w.nchunks, gpu.RESULT_DTYPE)
+    bufs = [np.zeros(1 << 22, np.int16), np.zeros(1 << 22, np.int16), np.zeros(1 << 21, np.uint32)]
+    dw.rebuild_to_host(3, *bufs, res, slabs=2)
+    assert _same_outputs(want[3][0], want[3][1], res, bufs) is None

@@ -33,6 +33,23 @@ int vpi_cuda_fail(cudaError_t e, const char *what)
 	return e == cudaErrorMemoryAllocation ? VP_ENOMEM : VP_ECUDA;
 }
 
+/* A few words between device and host as kernels: stores into mapped pinned
+ * memory do not queue behind bulk transfers on the copy engines, as a small
+ * cudaMemcpyAsync would while an output readback is in flight. */
+template <typename T> __global__ void k_fetch_words(const T *src, T *dst, uint32_t n)
+{
+	if (threadIdx.x < n) dst[threadIdx.x] = src[threadIdx.x];
+}
+
+__global__ void k_put_cursors(unsigned long long *cur, unsigned long long a, unsigned long long b, unsigned long long c)
+{
+	if (threadIdx.x == 0) {
+		cur[0] = a;
+		cur[1] = b;
+		cur[2] = c;
+	}
+}
+
 extern "C" {
 
 VP_API const char *vp_strerror(int code)
@@ -247,9 +264,17 @@ VP_API void vp_world_destroy(vp_world *w)
 		cudaStreamSynchronize(w->copy_stream);
 		cudaStreamDestroy(w->copy_stream);
 	}
+	for (int h = 0; h < 2; h++)
+		if (w->half_done[h]) cudaEventDestroy(w->half_done[h]);
+	if (w->outs_alt[1]) {
+		/* one of the two record buffers is d_outs (freed below) */
+		if (w->outs_alt[1] != w->d_outs) dev_free(w->outs_alt[1]);
+		else dev_free(w->outs_alt[0]);
+	}
 	for (int k = 0; k < kMaxStreamSlabs; k++)
 		if (w->slab_ev[k]) cudaEventDestroy(w->slab_ev[k]);
 	if (w->h_snap) cudaFreeHost(w->h_snap);
+	if (w->h_check) cudaFreeHost(w->h_check);
 	dev_free(w->d_set);
 	dev_free(w->d_items);
 	dev_free(w->d_outs);
@@ -362,7 +387,11 @@ VP_API int vp_world_upload(vp_world *w, const uint32_t *pool, uint64_t pool_word
 		if ((rc = dev_alloc(&w->d_shadow, shadow_len + 8))) return rc;
 		w->shadow_cap = shadow_len + 8;
 	}
-	if (!w->d_check && (rc = dev_alloc(&w->d_check, 2))) return rc;
+	if (!w->d_check) {
+		if ((rc = dev_alloc(&w->d_check, 2))) return rc;
+		CK(cudaHostAlloc((void **)&w->h_check, 2 * sizeof(uint32_t), cudaHostAllocMapped));
+		CK(cudaHostGetDevicePointer((void **)&w->h_check_dev, w->h_check, 0));
+	}
 	CK(cudaMemcpyAsync(w->d_pool, src, words * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
 	CK(cudaMemsetAsync(w->d_pool + words, 0, 8 * sizeof(uint32_t), st));
 	w->pool_tail = total;
@@ -378,10 +407,10 @@ VP_API int vp_world_upload(vp_world *w, const uint32_t *pool, uint64_t pool_word
 	cudaError_t e = launch_validate_streams(w->d_pool, w->d_off, w->d_len, w->nchunks, N, w->d_check,
 						w->d_check + 1, st);
 	if (e != cudaSuccess) return cuda_fail(e, "stream validation");
-	uint32_t chk[2];
-	CK(cudaMemcpyAsync(chk, w->d_check, sizeof(chk), cudaMemcpyDeviceToHost, st));
+	k_fetch_words<<<1, 32, 0, st>>>(w->d_check, w->h_check_dev, 2u);
+	CK(cudaGetLastError());
 	CK(cudaStreamSynchronize(st));
-	if (chk[0]) {
+	if (w->h_check[0]) {
 		w->uploaded = false;
 		return VP_EINVAL;
 	}
@@ -551,6 +580,8 @@ VP_API int vp_world_reserve(vp_world *w, const uint64_t bytes[3])
 	if (!w || !bytes) return VP_EINVAL;
 	CK(cudaSetDevice(w->ctx->device));
 	CK(cudaStreamSynchronize(w->ctx->stream));
+	int rc0 = vpi_pipe_drain(w);
+	if (rc0) return rc0;
 	for (int a = 0; a < 3; a++) {
 		const uint64_t units = std::max<uint64_t>((bytes[a] + 15u) / 16u, 1u);
 		dev_free(w->d_arena[a]);
@@ -565,7 +596,7 @@ VP_API int vp_world_reserve(vp_world *w, const uint64_t bytes[3])
 	return VP_OK;
 }
 
-static int enqueue_group(vp_world *w, int lod_max)
+static int enqueue_group(vp_world *w, int lod_max, uint64_t svl_cap_units)
 {
 	cudaStream_t st = w->ctx->stream;
 	const size_t L = (size_t)VP_MAX_LEVELS, n = w->nchunks;
@@ -591,7 +622,7 @@ static int enqueue_group(vp_world *w, int lod_max)
 	a.svl = (const int16_t *)w->d_arena[0];
 	a.out = w->d_garena;
 	a.svl_cursor = w->d_cursors;
-	a.svl_cap_units = w->cap[0];
+	a.svl_cap_units = svl_cap_units;
 	a.out_cap = (uint64_t)w->garena_units * 8u;
 	cudaError_t e = launch_group(w->d_outs, w->nchunks, lod_max, a, st);
 	if (e != cudaSuccess) return cuda_fail(e, "group launch");
@@ -605,6 +636,7 @@ static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 	vp_ctx *ctx = w->ctx;
 	cudaStream_t st = ctx->stream;
 	int rc;
+	if ((rc = vpi_pipe_drain(w))) return rc;
 	if ((rc = ensure_items(w)) || (rc = vpi_ensure_arenas(w))) return rc;
 	CK(cudaMemsetAsync(w->d_cursors, 0, 3 * sizeof(unsigned long long), st));
 	CK(cudaMemsetAsync(w->d_queue, 0, sizeof(unsigned int), st));
@@ -678,7 +710,7 @@ static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 	if (ctx->timing) cudaEventRecord(e2, st);
 	w->grouped_lod = -1;
 	if (flags & VP_REBUILD_GROUP) {
-		int rc2 = enqueue_group(w, lod_max);
+		int rc2 = enqueue_group(w, lod_max, w->cap[0]);
 		if (rc2) return rc2;
 	}
 	if (ctx->timing) {
@@ -988,20 +1020,49 @@ VP_API int vp_world_render(vp_world *w, const vp_camera *cam, const uint32_t *me
 	return (big[0] > big_cap || big[1] > big_cap) ? VP_EOVERFLOW : VP_OK;
 }
 
-VP_API int vp_world_rebuild_to_host(vp_world *w, int lod_max, unsigned flags, int slabs, void *svl,
-				    uint64_t svl_bytes, void *vbo, uint64_t vbo_bytes, void *ibo, uint64_t ibo_bytes,
-				    vp_chunk_result *results, uint64_t used_bytes[3])
+/* Pipelined rebuild into half h: wait for its copies and rebase the result
+ * records they delivered (device offsets index the whole arena; host
+ * offsets index the host buffers, which start at the half's base). */
+static int settle_half(vp_world *w, int h)
 {
-	if (!w || !w->uploaded || !results || !used_bytes) return VP_EINVAL;
-	if (lod_max < 0 || lod_max >= VP_MAX_LEVELS || slabs < 1 || slabs > kMaxStreamSlabs) return VP_EINVAL;
-	if ((flags & VP_REBUILD_PLAIN) || w->root_bitw == 7) {
-		/* per-chunk launches and 128^3 chunks take the plain sequence */
-		int rc;
-		if ((rc = vp_world_rebuild(w, lod_max, flags)) || (rc = vp_world_finish(w)) ||
-		    (rc = vp_world_results(w, results, w->nchunks)))
-			return rc;
-		return vp_world_read_outputs(w, svl, svl_bytes, vbo, vbo_bytes, ibo, ibo_bytes, used_bytes);
+	if (!w->half_busy[h]) return VP_OK;
+	CK(cudaEventSynchronize(w->half_done[h]));
+	vp_world::Rebase &rb = w->rebase[h];
+	for (uint32_t c = 0; c < rb.n; c++) {
+		vp_chunk_result &r = rb.res[c];
+		if (r.svl_total) r.svl_off -= rb.base[0] * 8u;
+		if (r.vbo_items) r.vbo_off -= rb.base[1] * 8u;
+		if (r.ibo_items) r.ibo_off -= rb.base[2] * 4u;
 	}
+	rb.res = nullptr;
+	rb.n = 0;
+	w->half_busy[h] = false;
+	return VP_OK;
+}
+
+int vpi_pipe_drain(vp_world *w)
+{
+	int rc;
+	const int older = w->pipe_half; /* the next half to be used was written first */
+	if ((rc = settle_half(w, older)) || (rc = settle_half(w, older ^ 1))) return rc;
+	return VP_OK;
+}
+
+VP_API int vp_world_outputs_wait(vp_world *w)
+{
+	if (!w) return VP_EINVAL;
+	CK(cudaSetDevice(w->ctx->device));
+	return vpi_pipe_drain(w);
+}
+
+/* The streamed rebuild. Synchronous: the whole arenas, everything finished
+ * on return. Pipelined: the arenas' half `pipe_half` and its own result
+ * records; returns once this call's copies are issued and the previous
+ * call's copies (which ran under this call's compute) have finished. */
+static int stream_rebuild(vp_world *w, int lod_max, unsigned flags, int slabs, void *svl, uint64_t svl_bytes,
+			  void *vbo, uint64_t vbo_bytes, void *ibo, uint64_t ibo_bytes, vp_chunk_result *results,
+			  uint64_t used_bytes[3], bool pipelined)
+{
 	CK(cudaSetDevice(w->ctx->device));
 	vp_ctx *ctx = w->ctx;
 	cudaStream_t st = ctx->stream;
@@ -1010,9 +1071,29 @@ VP_API int vp_world_rebuild_to_host(vp_world *w, int lod_max, unsigned flags, in
 	if (!w->copy_stream) {
 		CK(cudaStreamCreateWithFlags(&w->copy_stream, cudaStreamNonBlocking));
 		for (int k = 0; k < kMaxStreamSlabs; k++) CK(cudaEventCreateWithFlags(&w->slab_ev[k], cudaEventDisableTiming));
-		CK(cudaHostAlloc((void **)&w->h_snap, 3u * kMaxStreamSlabs * sizeof(unsigned long long), cudaHostAllocDefault));
+		for (int h = 0; h < 2; h++) CK(cudaEventCreateWithFlags(&w->half_done[h], cudaEventDisableTiming));
+		CK(cudaHostAlloc((void **)&w->h_snap, 3u * kMaxStreamSlabs * sizeof(unsigned long long),
+				 cudaHostAllocMapped));
+		CK(cudaHostGetDevicePointer((void **)&w->h_snap_dev, w->h_snap, 0));
 		if ((rc = dev_alloc(&w->d_slab_q, kMaxStreamSlabs)) || (rc = dev_alloc(&w->d_stream_items, w->nchunks)))
 			return rc;
+	}
+	if (!pipelined && (rc = vpi_pipe_drain(w))) return rc;
+	const int h = pipelined ? w->pipe_half : 0;
+	uint64_t base[3] = {0, 0, 0}, limit[3];
+	for (int a = 0; a < 3; a++) {
+		const uint64_t half = w->cap[a] / 2u;
+		base[a] = pipelined ? (uint64_t)h * half : 0u;
+		limit[a] = pipelined ? base[a] + half : w->cap[a];
+	}
+	if (pipelined) {
+		if (!w->outs_alt[1]) {
+			w->outs_alt[0] = w->d_outs;
+			if ((rc = dev_alloc(&w->outs_alt[1], w->nchunks))) return rc;
+		}
+		/* this half was last written two calls ago: its copies end first */
+		if ((rc = settle_half(w, h))) return rc;
+		w->d_outs = w->outs_alt[h];
 	}
 	/* slab k takes ranks k, k + S, k + 2S, ... of the longest-first order, so
 	 * every slab holds a similar mix and is itself longest first */
@@ -1028,7 +1109,8 @@ VP_API int vp_world_rebuild_to_host(vp_world *w, int lod_max, unsigned flags, in
 		w->stream_slabs = slabs;
 	}
 	for (int k = 0; k < slabs; k++) first[k + 1] = first[k] + (w->nchunks - (uint32_t)k + (uint32_t)slabs - 1) / slabs;
-	CK(cudaMemsetAsync(w->d_cursors, 0, 3 * sizeof(unsigned long long), st));
+	k_put_cursors<<<1, 32, 0, st>>>(w->d_cursors, base[0], base[1], base[2]);
+	CK(cudaGetLastError());
 	CK(cudaMemsetAsync(w->d_slab_q, 0, kMaxStreamSlabs * sizeof(unsigned int), st));
 	GeoLaunch L;
 	memset(&L, 0, sizeof(L));
@@ -1043,7 +1125,7 @@ VP_API int vp_world_rebuild_to_host(vp_world *w, int lod_max, unsigned flags, in
 	Arena *ar[3] = {&L.svl, &L.vbo, &L.ibo};
 	for (int a = 0; a < 3; a++) {
 		ar[a]->base = w->d_arena[a];
-		ar[a]->cap_units = w->cap[a];
+		ar[a]->cap_units = limit[a];
 		ar[a]->cursor = w->d_cursors + a;
 	}
 	const int per_sm = geometry_ctas_per_sm(w->root_bitw, (int)L.threads);
@@ -1059,48 +1141,111 @@ VP_API int vp_world_rebuild_to_host(vp_world *w, int lod_max, unsigned flags, in
 		Lg.queue = w->d_slab_q + k;
 		e = launch_geometry(w->root_bitw, Lg, st);
 		if (e != cudaSuccess) return cuda_fail(e, "geometry launch");
-		CK(cudaMemcpyAsync(w->h_snap + 3 * k, w->d_cursors, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-				   st));
+		k_fetch_words<<<1, 32, 0, st>>>(w->d_cursors, w->h_snap_dev + 3 * k, 3u);
+		CK(cudaGetLastError());
 		CK(cudaEventRecord(w->slab_ev[k], st));
 	}
 	w->launches += 1 + slabs;
 	w->grouped_lod = -1;
-	if ((flags & VP_REBUILD_GROUP) && (rc = enqueue_group(w, lod_max))) return rc;
+	if ((flags & VP_REBUILD_GROUP) && (rc = enqueue_group(w, lod_max, limit[0]))) return rc;
 	w->last_lod = lod_max;
 	w->last_flags = flags;
 	/* each slab's new output ranges go back while the next slab computes */
 	void *dst[3] = {svl, vbo, ibo};
 	const uint64_t cap_b[3] = {svl_bytes, vbo_bytes, ibo_bytes};
-	uint64_t prev[3] = {0, 0, 0};
+	uint64_t prev[3] = {base[0], base[1], base[2]};
 	bool overflow = false, short_buf = false;
 	for (int k = 0; k < slabs; k++) {
 		CK(cudaEventSynchronize(w->slab_ev[k]));
 		for (int a = 0; a < 3; a++) {
 			const uint64_t cur = w->h_snap[3 * k + a];
-			if (cur > w->cap[a]) overflow = true;
+			if (cur > limit[a]) overflow = true;
 			if (overflow || cur <= prev[a]) continue;
-			if (!dst[a] || cur * 16u > cap_b[a]) {
-				short_buf = short_buf || (cur * 16u > cap_b[a] && dst[a]);
+			const uint64_t end_b = (cur - base[a]) * 16u;
+			if (!dst[a] || end_b > cap_b[a]) {
+				short_buf = short_buf || (dst[a] && end_b > cap_b[a]);
 				prev[a] = cur;
 				continue;
 			}
-			CK(cudaMemcpyAsync((uint8_t *)dst[a] + prev[a] * 16u, (const uint8_t *)w->d_arena[a] + prev[a] * 16u,
-					   (cur - prev[a]) * 16u, cudaMemcpyDeviceToHost, w->copy_stream));
+			CK(cudaMemcpyAsync((uint8_t *)dst[a] + (prev[a] - base[a]) * 16u,
+					   (const uint8_t *)w->d_arena[a] + prev[a] * 16u, (cur - prev[a]) * 16u,
+					   cudaMemcpyDeviceToHost, w->copy_stream));
 			prev[a] = cur;
 		}
 	}
 	if (overflow) {
-		/* an arena was too small: grow it and run the plain sequence */
+		/* an arena (half) was too small: size each arena for twice what
+		 * this rebuild asked for and run it again */
+		uint64_t need[3];
+		for (int a = 0; a < 3; a++) need[a] = w->h_snap[3 * (slabs - 1) + a] - base[a];
+		CK(cudaStreamSynchronize(st));
 		CK(cudaStreamSynchronize(w->copy_stream));
-		if ((rc = vp_world_finish(w)) || (rc = vp_world_results(w, results, w->nchunks))) return rc;
-		return vp_world_read_outputs(w, svl, svl_bytes, vbo, vbo_bytes, ibo, ibo_bytes, used_bytes);
+		if ((rc = vpi_pipe_drain(w))) return rc;
+		for (int a = 0; a < 3; a++) {
+			const uint64_t want = (need[a] + need[a] / 4 + 1024) * (pipelined ? 2u : 1u);
+			if (want <= w->cap[a]) continue;
+			dev_free(w->d_arena[a]);
+			w->cap[a] = 0;
+			cudaError_t e2 = cudaMalloc(&w->d_arena[a], want * 16u);
+			if (e2 != cudaSuccess) {
+				w->d_arena[a] = nullptr;
+				return cuda_fail(e2, "cudaMalloc(arena growth)");
+			}
+			w->cap[a] = want;
+		}
+		w->pipe_half = 0;
+		return stream_rebuild(w, lod_max, flags, slabs, svl, svl_bytes, vbo, vbo_bytes, ibo, ibo_bytes, results,
+				      used_bytes, pipelined);
 	}
 	CK(cudaMemcpyAsync(results, w->d_outs, (size_t)w->nchunks * sizeof(ChunkOut), cudaMemcpyDeviceToHost,
 			   w->copy_stream));
+	for (int a = 0; a < 3; a++) used_bytes[a] = (prev[a] - base[a]) * 16u;
+	if (pipelined) {
+		CK(cudaEventRecord(w->half_done[h], w->copy_stream));
+		w->half_busy[h] = true;
+		vp_world::Rebase &rb = w->rebase[h];
+		rb.res = results;
+		rb.n = w->nchunks;
+		for (int a = 0; a < 3; a++) rb.base[a] = base[a];
+		w->pipe_half = h ^ 1;
+		/* the previous call's copies ran under this call's compute */
+		if ((rc = settle_half(w, h ^ 1))) return rc;
+		return short_buf ? VP_EOVERFLOW : VP_OK;
+	}
 	CK(cudaStreamSynchronize(w->copy_stream));
 	CK(cudaStreamSynchronize(st));
-	for (int a = 0; a < 3; a++) used_bytes[a] = prev[a] * 16u;
 	return short_buf ? VP_EOVERFLOW : VP_OK;
+}
+
+VP_API int vp_world_rebuild_to_host(vp_world *w, int lod_max, unsigned flags, int slabs, void *svl,
+				    uint64_t svl_bytes, void *vbo, uint64_t vbo_bytes, void *ibo, uint64_t ibo_bytes,
+				    vp_chunk_result *results, uint64_t used_bytes[3])
+{
+	if (!w || !w->uploaded || !results || !used_bytes) return VP_EINVAL;
+	if (lod_max < 0 || lod_max >= VP_MAX_LEVELS || slabs < 1 || slabs > kMaxStreamSlabs) return VP_EINVAL;
+	if ((flags & VP_REBUILD_PLAIN) || w->root_bitw == 7) {
+		/* per-chunk launches and 128^3 chunks take the plain sequence */
+		int rc;
+		if ((rc = vp_world_rebuild(w, lod_max, flags)) || (rc = vp_world_finish(w)) ||
+		    (rc = vp_world_results(w, results, w->nchunks)))
+			return rc;
+		return vp_world_read_outputs(w, svl, svl_bytes, vbo, vbo_bytes, ibo, ibo_bytes, used_bytes);
+	}
+	return stream_rebuild(w, lod_max, flags, slabs, svl, svl_bytes, vbo, vbo_bytes, ibo, ibo_bytes, results,
+			      used_bytes, false);
+}
+
+VP_API int vp_world_rebuild_to_host_async(vp_world *w, int lod_max, unsigned flags, int slabs, void *svl,
+					  uint64_t svl_bytes, void *vbo, uint64_t vbo_bytes, void *ibo,
+					  uint64_t ibo_bytes, vp_chunk_result *results, uint64_t used_bytes[3])
+{
+	if (!w || !w->uploaded || !results || !used_bytes) return VP_EINVAL;
+	if (lod_max < 0 || lod_max >= VP_MAX_LEVELS || slabs < 1 || slabs > kMaxStreamSlabs) return VP_EINVAL;
+	if ((flags & VP_REBUILD_PLAIN) || w->root_bitw == 7)
+		return vp_world_rebuild_to_host(w, lod_max, flags, slabs, svl, svl_bytes, vbo, vbo_bytes, ibo, ibo_bytes,
+						results, used_bytes);
+	return stream_rebuild(w, lod_max, flags, slabs, svl, svl_bytes, vbo, vbo_bytes, ibo, ibo_bytes, results,
+			      used_bytes, true);
 }
 
 VP_API int vp_world_results(vp_world *w, vp_chunk_result *out, uint32_t n)

@@ -63,6 +63,8 @@ struct vp_world {
 	uint64_t shadow_len = 0;
 	uint64_t shadow_cap = 0;                 /* elements allocated in d_shadow */
 	uint32_t *d_check = nullptr;             /* upload validation: status, first bad chunk */
+	uint32_t *h_check = nullptr;             /* its mapped pinned copy, and that copy's device address */
+	uint32_t *h_check_dev = nullptr;
 	/* draw culling */
 	uint32_t *d_cull_slots = nullptr;
 	uint64_t cull_slots_cap = 0;
@@ -84,7 +86,18 @@ struct vp_world {
 	unsigned int *d_slab_q = nullptr;
 	cudaStream_t copy_stream = nullptr;
 	cudaEvent_t slab_ev[kMaxStreamSlabs] = {};
-	unsigned long long *h_snap = nullptr;   /* pinned: 3 cursors per slab */
+	unsigned long long *h_snap = nullptr;   /* mapped pinned: 3 cursors per slab */
+	unsigned long long *h_snap_dev = nullptr;
+	/* pipelined streamed rebuilds: arena halves and result records alternate */
+	ChunkOut *outs_alt[2] = {nullptr, nullptr};
+	int pipe_half = 0;
+	bool half_busy[2] = {false, false};
+	cudaEvent_t half_done[2] = {nullptr, nullptr};
+	struct Rebase {
+		vp_chunk_result *res = nullptr;
+		uint32_t n = 0;
+		uint64_t base[3] = {0, 0, 0};
+	} rebase[2];
 	uint8_t *d_render = nullptr;            /* queues, segments, scans, big lists */
 	size_t render_cap = 0;
 	uint8_t *d_frame = nullptr;             /* frame words, RGBA, depth */
@@ -162,4 +175,6 @@ int vpi_world_shadow_window(vp_world *w, const uint16_t *map, uint64_t map_len, 
 int vpi_world_run(vp_world *w, const WorkItem *items, uint32_t n, int lod_max);
 /* A reference-format stream of n words (terminator included) covering N
  * voxels with nonzero run lengths. */
+/* waits for the copies of pipelined streamed rebuilds and rebases their results */
+extern "C" int vpi_pipe_drain(vp_world *w);
 extern "C" int vpi_validate_stream(const uint32_t *s, uint32_t n, uint64_t N);

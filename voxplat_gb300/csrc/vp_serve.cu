@@ -326,7 +326,9 @@ VP_API int vp_world_edit(vp_world *w, const vp_edit *edits, uint32_t n)
 {
 	if (!w || (!edits && n) || !w->uploaded) return VP_EINVAL;
 	CK(cudaSetDevice(w->ctx->device));
-	int rc = enqueue_batch(w, edits, n);
+	int rc = vpi_pipe_drain(w);
+	if (rc) return rc;
+	rc = enqueue_batch(w, edits, n);
 	if (!rc) rc = finish_batch(w);
 	return rc;
 }
@@ -382,6 +384,8 @@ VP_API int vp_world_serve(vp_world *w, const vp_edit *edits, uint32_t n, uint32_
 	if (!w || (!edits && n) || !latency_ms || !stats || !w->uploaded || !max_batch) return VP_EINVAL;
 	CK(cudaSetDevice(w->ctx->device));
 	memset(stats, 0, sizeof(*stats));
+	const int rc0 = vpi_pipe_drain(w);
+	if (rc0) return rc0;
 	std::vector<uint32_t> queue, batch;
 	size_t qhead = 0;
 	uint32_t next = 0, done = 0;

@@ -132,6 +132,8 @@ def load(build_if_missing=True):
         "vp_world_results": (I, [V, V, U32]),
         "vp_world_read_outputs": (I, [V, V, U64, V, U64, V, U64, V]),
         "vp_world_rebuild_to_host": (I, [V, I, ctypes.c_uint, I, V, U64, V, U64, V, U64, V, V]),
+        "vp_world_rebuild_to_host_async": (I, [V, I, ctypes.c_uint, I, V, U64, V, U64, V, U64, V, V]),
+        "vp_world_outputs_wait": (I, [V]),
         "vp_world_cull": (I, [V, V, V, I, V, U32, ctypes.POINTER(U32), V, U32, ctypes.POINTER(U32)]),
         "vp_world_camera_modes": (I, [V, V, V]),
         "vp_world_raycast": (I, [V, U32, V, V, V, V, V]),
@@ -340,6 +342,22 @@ class DeviceWorld:
                                                 vbo.nbytes, _p(ibo), ibo.nbytes, _p(results), _p(used)),
               "vp_world_rebuild_to_host")
         return [int(u) for u in used]
+
+    def rebuild_to_host_async(self, lod_max, svl, vbo, ibo, results, group=False, slabs=4):
+        """rebuild_to_host pipelined with the next call: returns once the
+        copies are issued. The arrays stay in use until outputs_wait() (or
+        any other call on this world) returns; successive calls must
+        alternate between two sets of arrays."""
+        used = np.zeros(3, np.uint64)
+        flags = VP_REBUILD_PERSISTENT | (VP_REBUILD_GROUP if group else 0)
+        check(self.lib.vp_world_rebuild_to_host_async(self.h, lod_max, flags, slabs, _p(svl), svl.nbytes,
+                                                      _p(vbo), vbo.nbytes, _p(ibo), ibo.nbytes, _p(results),
+                                                      _p(used)),
+              "vp_world_rebuild_to_host_async")
+        return [int(u) for u in used]
+
+    def outputs_wait(self):
+        check(self.lib.vp_world_outputs_wait(self.h), "vp_world_outputs_wait")
 
     def read_outputs(self, svl, vbo, ibo):
         """Copy the used part of the three output arenas into the given
