@@ -64,7 +64,8 @@ struct Geo {
 		return t > groups_of(RR) ? t : groups_of(RR);
 	}
 	static constexpr size_t o_grp = a16(o_tmp + sizeof(uint32_t) * 64);
-	static constexpr size_t o_e0p = a16(o_grp + sizeof(uint32_t) * (max_groups() + 1));
+	static constexpr size_t o_glist = a16(o_grp + sizeof(uint32_t) * (max_groups() + 1));
+	static constexpr size_t o_e0p = a16(o_glist + sizeof(uint16_t) * max_groups());
 	static constexpr size_t o_sv = a16(o_e0p + sizeof(uint64_t) * 3 * R);
 	static constexpr size_t o_nbr = a16(o_sv + sizeof(uint64_t) * 2 * R);
 	static constexpr size_t bytes = a16(o_nbr + sizeof(int32_t) * 28);
@@ -76,6 +77,7 @@ struct Smem {
 	uint64_t *occ, *rs, *lv;
 	uint32_t *rank, *tmp;
 	uint32_t *grp;   /* emission base of every 32-row group */
+	uint16_t *glist; /* the groups with any output, in order */
 	uint64_t *e0p;   /* splat mode: L0 mask rows of the x = R, y = R, z = R planes */
 	uint64_t *sv;    /* splat mode: two saved occupancy planes */
 	uint64_t *xrow;  /* [side][z+1]: x = -1 (side 0) / x = R (side 1), bits over y */
@@ -96,6 +98,7 @@ __device__ __forceinline__ Smem carve(uint8_t *base)
 	s.xedge = base + G::o_xedge;
 	s.tmp = (uint32_t *)(base + G::o_tmp);
 	s.grp = (uint32_t *)(base + G::o_grp);
+	s.glist = (uint16_t *)(base + G::o_glist);
 	s.e0p = (uint64_t *)(base + G::o_e0p);
 	s.sv = (uint64_t *)(base + G::o_sv);
 	s.nbr = (int32_t *)(base + G::o_nbr);
@@ -781,19 +784,30 @@ __device__ __forceinline__ void select_face(uint64_t fx, uint64_t fy, uint64_t f
 
 /* Exclusive scan, in place, of n <= 32*8 group counts by warp 0; returns
  * the total to all threads. */
-__device__ __forceinline__ uint32_t scan_groups(uint32_t *g, int n, uint32_t *tmp)
+/* Exclusive scan of the n group counts in place; returns the total. With a
+ * list, also writes the indices of the non-empty groups there, in order,
+ * and their number to tmp[1]. */
+__device__ __forceinline__ uint32_t scan_groups(uint32_t *g, int n, uint32_t *tmp, uint16_t *list = nullptr)
 {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	if (warp == 0) {
-		uint32_t carry = 0;
+		uint32_t carry = 0, listed = 0;
 		for (int b = 0; b < n; b += 32) {
 			const int i = b + lane;
 			const uint32_t v = i < n ? g[i] : 0u;
 			const uint32_t inc = warp_incl_add(v);
 			if (i < n) g[i] = carry + inc - v;
 			carry += __shfl_sync(kFull, inc, 31);
+			if (list) {
+				const uint32_t ne = __ballot_sync(kFull, v != 0u);
+				if (v) list[listed + __popc(ne & ((1u << lane) - 1u))] = (uint16_t)i;
+				listed += __popc(ne);
+			}
 		}
-		if (lane == 0) tmp[0] = carry;
+		if (lane == 0) {
+			tmp[0] = carry;
+			tmp[1] = listed;
+		}
 	}
 	__syncthreads();
 	const uint32_t t = tmp[0];
@@ -892,13 +906,14 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
  * {x, y, z, colour | shadow << 6} (src/chunkset/mesher.c:521-531). At each
  * level the eight child bits form a pattern indexed dx + 2 dy + 4 dz, and
  * the chosen child is its highest set bit. */
-template <int RB>
+template <int RB, int L>
 __device__ __forceinline__ void emit_splat(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m,
-					   const uint32_t cv[3], int l, int x, int y, int z, int16_t *dst, bool sh_in)
+					   const uint32_t cv[3], int x, int y, int z, int16_t *dst, bool sh_in)
 {
 	constexpr int R = Geo<RB>::R;
 	int cx = x, cy = y, cz = z;
-	for (int lc = l - 1; lc >= 0; lc--) {
+#pragma unroll
+	for (int lc = L - 1; lc >= 0; lc--) {
 		const int np = (R >> lc) + 1;
 		const int X = 2 * cx;
 		uint32_t pat = 0;
@@ -919,10 +934,10 @@ __device__ __forceinline__ void emit_splat(const SetDesc &S, const uint32_t *__r
 		cz = 2 * cz + (best >> 2);
 	}
 	const uint32_t colour = mask_colour<RB>(S, stream, m, cx, cy, cz);
-	const uint32_t sh = l ? (1u << l) : 0u;
-	const uint32_t wx = (cv[0] << RB) + ((uint32_t)x << l);
-	const uint32_t wy = (cv[1] << RB) + ((uint32_t)y << l);
-	const uint32_t wz = (cv[2] << RB) + ((uint32_t)z << l);
+	constexpr uint32_t sh = L ? (1u << L) : 0u;
+	const uint32_t wx = (cv[0] << RB) + ((uint32_t)x << L);
+	const uint32_t wy = (cv[1] << RB) + ((uint32_t)y << L);
+	const uint32_t wz = (cv[2] << RB) + ((uint32_t)z << L);
 	uint32_t shadow;
 	if (sh_in) {
 		/* the chunk's whole sample window lies inside the map: no bounds
@@ -948,6 +963,54 @@ __device__ __forceinline__ bool shadow_window_inside(const SetDesc &S, const uin
 	const uint64_t lo = x0 + y0 + (uint64_t)S.shadow_w * z0;
 	const uint64_t hi = (x0 + ext) + (y0 + ext) + (uint64_t)S.shadow_w * (z0 + ext) + 1u;
 	return hi < (1ull << 32) && lo >= S.shadow_base && hi - S.shadow_base < S.shadow_len;
+}
+
+/* Pass 2 of one non-empty 32-row group of level L: lane s holds row s and
+ * its exclusive item offset; items go one per lane per step, a second one
+ * when more than 32 remain (both searches first, so their shuffle chains
+ * overlap). Specialised per level, so the row division, the walk down and
+ * the shifts are compile-time. */
+template <int RB, int L>
+__device__ __forceinline__ void splat_group(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m,
+					    const uint32_t cv[3], int g, int16_t *dst, bool sh_in)
+{
+	constexpr int R = Geo<RB>::R;
+	constexpr uint32_t n = (uint32_t)(R >> L) + 1u;
+	const int lane = threadIdx.x & 31;
+	const uint32_t r = (uint32_t)(g - c_lv.gstart[RB][L]) * 32u + (uint32_t)lane;
+	uint64_t row = 0;
+	uint32_t xr = 0, yz = 0;
+	if (r < n * n) {
+		const uint32_t z = r / n, y = r - z * n;
+		row = level_row<RB>(m, L, (int)y, (int)z, xr);
+		yz = y | (z << 16);
+	}
+	const uint32_t c = __popcll(row) + xr;
+	const uint32_t inc = warp_incl_add(c);
+	const uint32_t excl = inc - c;
+	const uint32_t T = __shfl_sync(kFull, inc, 31);
+	const uint32_t base = m.grp[g];
+	for (uint32_t k = 0; k < T; k += 64) {
+		const bool two = k + 32 < T;
+		const uint32_t j0 = k + lane, j1 = k + 32 + lane;
+		const int s0 = search_lane(excl, j0);
+		const int s1 = two ? search_lane(excl, j1) : 0;
+		const uint32_t e0 = __shfl_sync(kFull, excl, s0), q0 = __shfl_sync(kFull, yz, s0);
+		const uint32_t e1 = __shfl_sync(kFull, excl, s1), q1 = __shfl_sync(kFull, yz, s1);
+		const uint64_t w0 = shfl64(row, s0), w1 = shfl64(row, s1);
+		if (j0 < T) {
+			const int kk = (int)(j0 - e0);
+			const int x = kk < __popcll(w0) ? select_bit(w0, kk) : R;
+			emit_splat<RB, L>(S, stream, m, cv, x, (int)(q0 & 0xFFFFu), (int)(q0 >> 16),
+					  dst + (size_t)(base + j0) * 4, sh_in);
+		}
+		if (two && j1 < T) {
+			const int kk = (int)(j1 - e1);
+			const int x = kk < __popcll(w1) ? select_bit(w1, kk) : R;
+			emit_splat<RB, L>(S, stream, m, cv, x, (int)(q1 & 0xFFFFu), (int)(q1 >> 16),
+					  dst + (size_t)(base + j1) * 4, sh_in);
+		}
+	}
 }
 
 template <int RB>
@@ -1004,7 +1067,8 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 		if (lane == 0) m.grp[g] = c;
 	}
 	__syncthreads();
-	const uint32_t total = scan_groups(m.grp, ngroups, m.tmp);
+	const uint32_t total = scan_groups(m.grp, ngroups, m.tmp, m.glist);
+	const uint32_t listed = m.tmp[1];
 	if (threadIdx.x == 0) {
 		const uint64_t units = ((uint64_t)total + 1u) / 2u; /* 8 B per splat */
 		unsigned long long b = units ? atomicAdd(asvl.cursor, (unsigned long long)units) : 0ull;
@@ -1031,52 +1095,26 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 	if (!s_ok) return;
 	int16_t *dst = (int16_t *)asvl.base + s_base * 8u;
 	const bool sh_in = shadow_window_inside<RB>(S, cv, lod_max);
-	/* pass 2: warps take groups from a shared counter; one splat per lane
-	 * per step, a second one when the group has more than 32 left */
+	/* pass 2: warps take the non-empty groups from a shared counter */
+	static_assert(kMaxLevels == 8, "one splat_group case per level");
 	for (;;) {
-		uint32_t g = 0;
-		if (lane == 0) g = atomicAdd(&s_next, 1u);
-		g = __shfl_sync(kFull, g, 0);
-		if (g >= (uint32_t)ngroups) break;
+		uint32_t k = 0;
+		if (lane == 0) k = atomicAdd(&s_next, 1u);
+		k = __shfl_sync(kFull, k, 0);
+		if (k >= listed) break;
+		const int g = m.glist[k];
 		int l = 0;
-		while ((int)g >= gstart[l + 1]) l++;
-		const int n = (R >> l) + 1;
-		const int r = ((int)g - gstart[l]) * 32 + lane;
-		uint64_t row = 0;
-		uint32_t xr = 0, yz = 0;
-		if (r < n * n) {
-			int y, z;
-			row_yz((uint32_t)r, (uint32_t)n, c_lv.magic[RB][l], y, z);
-			row = level_row<RB>(m, l, y, z, xr);
-			yz = (uint32_t)y | ((uint32_t)z << 16);
-		}
-		const uint32_t c = __popcll(row) + xr;
-		const uint32_t inc = warp_incl_add(c);
-		const uint32_t excl = inc - c;
-		const uint32_t T = __shfl_sync(kFull, inc, 31);
-		const uint32_t base = m.grp[g];
-		for (uint32_t k = 0; k < T; k += 64) {
-			/* two items per lane when more than 32 remain: both searches
-			 * first, so their shuffle chains overlap */
-			const bool two = k + 32 < T;
-			const uint32_t j0 = k + lane, j1 = k + 32 + lane;
-			const int s0 = search_lane(excl, j0);
-			const int s1 = two ? search_lane(excl, j1) : 0;
-			const uint32_t e0 = __shfl_sync(kFull, excl, s0), q0 = __shfl_sync(kFull, yz, s0);
-			const uint32_t e1 = __shfl_sync(kFull, excl, s1), q1 = __shfl_sync(kFull, yz, s1);
-			const uint64_t w0 = shfl64(row, s0), w1 = shfl64(row, s1);
-			if (j0 < T) {
-				const int kk = (int)(j0 - e0);
-				const int x = kk < __popcll(w0) ? select_bit(w0, kk) : R;
-				emit_splat<RB>(S, stream, m, cv, l, x, (int)(q0 & 0xFFFFu), (int)(q0 >> 16),
-					       dst + (size_t)(base + j0) * 4, sh_in);
-			}
-			if (two && j1 < T) {
-				const int kk = (int)(j1 - e1);
-				const int x = kk < __popcll(w1) ? select_bit(w1, kk) : R;
-				emit_splat<RB>(S, stream, m, cv, l, x, (int)(q1 & 0xFFFFu), (int)(q1 >> 16),
-					       dst + (size_t)(base + j1) * 4, sh_in);
-			}
+#pragma unroll
+		for (int i = 1; i < kMaxLevels; i++) l += g >= c_lv.gstart[RB][i] ? 1 : 0;
+		switch (l) {
+		case 0: splat_group<RB, 0>(S, stream, m, cv, g, dst, sh_in); break;
+		case 1: splat_group<RB, 1>(S, stream, m, cv, g, dst, sh_in); break;
+		case 2: splat_group<RB, 2>(S, stream, m, cv, g, dst, sh_in); break;
+		case 3: splat_group<RB, 3>(S, stream, m, cv, g, dst, sh_in); break;
+		case 4: splat_group<RB, 4>(S, stream, m, cv, g, dst, sh_in); break;
+		case 5: splat_group<RB, 5>(S, stream, m, cv, g, dst, sh_in); break;
+		case 6: splat_group<RB, 6>(S, stream, m, cv, g, dst, sh_in); break;
+		default: splat_group<RB, 7>(S, stream, m, cv, g, dst, sh_in); break;
 		}
 	}
 }
