@@ -755,29 +755,43 @@ __device__ __forceinline__ void face_bits(const Smem &m, int y, int z, uint64_t 
 	fz = o ^ m.occ[hidx<RB>(y, z + 1)];
 }
 
-/* (x, axis) of the k-th face of a row, faces ordered by x then axis. */
+/* (x, axis) of the k-th face of a row, faces ordered by x then axis. The
+ * count of faces at each x, fx + fy + fz, is held as two bit planes (its
+ * low bit and whether it is >= 2), so a prefix count is two popcounts; the
+ * search takes the 32-bit half first, then halves within it. */
 template <int RB>
 __device__ __forceinline__ void select_face(uint64_t fx, uint64_t fy, uint64_t fz, uint32_t k, int &x, int &i)
 {
-	constexpr int R = Geo<RB>::R;
+	const uint64_t fxy = fx ^ fy;
+	const uint64_t lo = fxy ^ fz, hi = (fx & fy) | (fz & fxy);
+	uint32_t l32 = (uint32_t)lo, h32 = (uint32_t)hi;
 	int pos = 0;
-#pragma unroll
-	for (int step = R / 2; step; step >>= 1) {
-		const int t = pos + step;
-		const uint64_t below = (1ull << t) - 1ull;
-		const uint32_t c = __popcll(fx & below) + __popcll(fy & below) + __popcll(fz & below);
-		if (c <= k) pos = t;
+	const uint32_t c32 = __popc(l32) + 2u * __popc(h32);
+	if (c32 <= k) {
+		k -= c32;
+		pos = 32;
+		l32 = (uint32_t)(lo >> 32);
+		h32 = (uint32_t)(hi >> 32);
 	}
-	const uint64_t below = pos ? ((1ull << pos) - 1ull) : 0ull;
-	uint32_t r = k - (__popcll(fx & below) + __popcll(fy & below) + __popcll(fz & below));
+#pragma unroll
+	for (int step = 16; step; step >>= 1) {
+		const uint32_t below = (1u << step) - 1u;
+		const uint32_t c = __popc(l32 & below) + 2u * __popc(h32 & below);
+		if (c <= k) {
+			k -= c;
+			pos += step;
+			l32 >>= step;
+			h32 >>= step;
+		}
+	}
 	const uint32_t b0 = (uint32_t)((fx >> pos) & 1ull), b1 = (uint32_t)((fy >> pos) & 1ull);
 	x = pos;
 	if (b0) {
-		if (r == 0) { i = 0; return; }
-		r--;
+		if (k == 0) { i = 0; return; }
+		k--;
 	}
 	if (b1) {
-		if (r == 0) { i = 1; return; }
+		if (k == 0) { i = 1; return; }
 	}
 	i = 2;
 }
@@ -833,12 +847,12 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
 			face_bits<RB>(m, r & (R - 1), r >> RB, fx, fy, fz);
 			c = __popcll(fx) + __popcll(fy) + __popcll(fz);
 		}
-#pragma unroll
-		for (int d = 16; d; d >>= 1) c += __shfl_xor_sync(kFull, c, d);
+		c = __reduce_add_sync(kFull, c);
 		if (lane == 0) m.grp[g] = c;
 	}
 	__syncthreads();
-	const uint32_t faces = scan_groups(m.grp, NG, m.tmp);
+	const uint32_t faces = scan_groups(m.grp, NG, m.tmp, m.glist);
+	const uint32_t listed = m.tmp[1];
 	if (threadIdx.x == 0) {
 		const uint64_t uv = (uint64_t)faces * 2u;             /* 32 B per face */
 		const uint64_t ui = ((uint64_t)faces * 24u + 15u) / 16u;
@@ -863,13 +877,14 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
 	int16_t *vbo = (int16_t *)avbo.base + s_base[0] * 8u;
 	uint32_t *ibo = (uint32_t *)aibo.base + s_base[1] * 4u;
 	const SmallAcc<RB> acc{S, stream, m};
-	/* pass 2: warps take 32-row groups from a shared counter; one face per
-	 * lane per step */
+	/* pass 2: warps take the non-empty 32-row groups from a shared counter;
+	 * one face per lane per step, a second one when more than 32 remain */
 	for (;;) {
-		uint32_t g = 0;
-		if (lane == 0) g = atomicAdd(&s_next, 1u);
-		g = __shfl_sync(kFull, g, 0);
-		if (g >= (uint32_t)NG) break;
+		uint32_t t = 0;
+		if (lane == 0) t = atomicAdd(&s_next, 1u);
+		t = __shfl_sync(kFull, t, 0);
+		if (t >= listed) break;
+		const uint32_t g = m.glist[t];
 		const int r = (int)g * 32 + lane;
 		uint64_t fx = 0, fy = 0, fz = 0;
 		if (r < RR) face_bits<RB>(m, r & (R - 1), r >> RB, fx, fy, fz);
@@ -879,8 +894,9 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
 		const uint32_t T = __shfl_sync(kFull, inc, 31);
 		const uint32_t base = m.grp[g];
 		for (uint32_t k = 0; k < T; k += 64) {
+			const bool two = k + 32 < T;
 			const uint32_t j0 = k + lane, j1 = k + 32 + lane;
-			const int s0 = search_lane(excl, j0), s1 = search_lane(excl, j1);
+			const int s0 = search_lane(excl, j0), s1 = two ? search_lane(excl, j1) : 0;
 			const uint32_t e0 = __shfl_sync(kFull, excl, s0), e1 = __shfl_sync(kFull, excl, s1);
 			const uint64_t ax = shfl64(fx, s0), ay = shfl64(fy, s0), az = shfl64(fz, s0);
 			const uint64_t bx = shfl64(fx, s1), by = shfl64(fy, s1), bz = shfl64(fz, s1);
@@ -890,7 +906,7 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
 				const int rr = (int)g * 32 + s0;
 				emit_face<RB>(acc, S, cv, x, rr & (R - 1), rr >> RB, i, base + j0, vbo, ibo);
 			}
-			if (j1 < T) {
+			if (two && j1 < T) {
 				int x, i;
 				select_face<RB>(bx, by, bz, j1 - e1, x, i);
 				const int rr = (int)g * 32 + s1;
@@ -965,6 +981,62 @@ __device__ __forceinline__ bool shadow_window_inside(const SetDesc &S, const uin
 	return hi < (1ull << 32) && lo >= S.shadow_base && hi - S.shadow_base < S.shadow_len;
 }
 
+static_assert(kMaxLevels == 8, "the level switches have one case per level");
+
+/* Level of 32-row emission group g. */
+template <int RB>
+__device__ __forceinline__ int group_level(int g)
+{
+	int l = 0;
+#pragma unroll
+	for (int i = 1; i < kMaxLevels; i++) l += g >= c_lv.gstart[RB][i] ? 1 : 0;
+	return l;
+}
+
+/* Level-L rows (L >= 1): the pairwise OR of the four child rows of level
+ * L - 1, compacted along x (src/chunkset/mesher.c:460-493 as occupancy). */
+template <int RB, int L>
+__device__ __forceinline__ void build_level(const Smem &m)
+{
+	constexpr int R = Geo<RB>::R;
+	constexpr uint32_t n = (uint32_t)(R >> L) + 1u, np = (uint32_t)(R >> (L - 1)) + 1u;
+	uint64_t *dst = m.lv + c_lv.off[RB][L];
+	for (uint32_t i = threadIdx.x; i < n * n; i += blockDim.x) {
+		const uint32_t z = i / n, y = i - z * n;
+		uint64_t acc = 0;
+		uint32_t accx = 0;
+#pragma unroll
+		for (uint32_t dz = 0; dz < 2; dz++)
+#pragma unroll
+			for (uint32_t dy = 0; dy < 2; dy++) {
+				const uint32_t yy = 2 * y + dy, zz = 2 * z + dz;
+				if (yy >= np || zz >= np) continue;
+				uint32_t xr;
+				acc |= level_row<RB>(m, L - 1, (int)yy, (int)zz, xr);
+				accx |= xr;
+			}
+		uint64_t row = compress_pairs(acc);
+		if (L == 1) row |= (uint64_t)accx << (R / 2);
+		dst[i] = row;
+	}
+}
+
+/* Cells of 32-row group g of level L (all lanes call; every lane gets it). */
+template <int RB, int L>
+__device__ __forceinline__ uint32_t count_group(const Smem &m, int g)
+{
+	constexpr int R = Geo<RB>::R;
+	constexpr uint32_t n = (uint32_t)(R >> L) + 1u;
+	const uint32_t r = (uint32_t)(g - c_lv.gstart[RB][L]) * 32u + (threadIdx.x & 31u);
+	uint32_t c = 0;
+	if (r < n * n) {
+		const uint32_t z = r / n, y = r - z * n;
+		uint32_t xr;
+		c = __popcll(level_row<RB>(m, L, (int)y, (int)z, xr)) + xr;
+	}
+	return __reduce_add_sync(kFull, c);
+}
+
 /* Pass 2 of one non-empty 32-row group of level L: lane s holds row s and
  * its exclusive item offset; items go one per lane per step, a second one
  * when more than 32 remain (both searches first, so their shuffle chains
@@ -1017,8 +1089,6 @@ template <int RB>
 __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m, const uint32_t cv[3],
 			    int lod_max, ChunkOut *out, const Arena &asvl)
 {
-	using G = Geo<RB>;
-	constexpr int R = G::R;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 	__shared__ unsigned long long s_base;
 	__shared__ uint32_t s_ok, s_next;
@@ -1026,44 +1096,31 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 	splat_prepare<RB>(m);
 	/* level rows: pairwise OR of the child rows, compacted along x */
 	for (int l = 1; l <= lod_max; l++) {
-		const int n = (R >> l) + 1, np = (R >> (l - 1)) + 1;
-		const uint32_t mg = c_lv.magic[RB][l];
-		uint64_t *dst = m.lv + c_lv.off[RB][l];
-		for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
-			int y, z;
-			row_yz((uint32_t)i, (uint32_t)n, mg, y, z);
-			uint64_t acc = 0;
-			uint32_t accx = 0;
-			for (int dz = 0; dz < 2; dz++)
-				for (int dy = 0; dy < 2; dy++) {
-					const int yy = 2 * y + dy, zz = 2 * z + dz;
-					if (yy >= np || zz >= np) continue;
-					uint32_t xr;
-					acc |= level_row<RB>(m, l - 1, yy, zz, xr);
-					accx |= xr;
-				}
-			uint64_t row = compress_pairs(acc);
-			if (l == 1) row |= (uint64_t)accx << (R / 2);
-			dst[i] = row;
+		switch (l) {
+		case 1: build_level<RB, 1>(m); break;
+		case 2: build_level<RB, 2>(m); break;
+		case 3: build_level<RB, 3>(m); break;
+		case 4: build_level<RB, 4>(m); break;
+		case 5: build_level<RB, 5>(m); break;
+		case 6: build_level<RB, 6>(m); break;
+		default: build_level<RB, 7>(m); break;
 		}
 		__syncthreads();
 	}
 	/* pass 1: splats per 32-row group, levels in order */
 	const int ngroups = gstart[lod_max + 1];
 	for (int g = warp; g < ngroups; g += nw) {
-		int l = 0;
-		while (g >= gstart[l + 1]) l++;
-		const int n = (R >> l) + 1;
-		const int r = (g - gstart[l]) * 32 + lane;
-		uint32_t c = 0;
-		if (r < n * n) {
-			int y, z;
-			row_yz((uint32_t)r, (uint32_t)n, c_lv.magic[RB][l], y, z);
-			uint32_t xr;
-			c = __popcll(level_row<RB>(m, l, y, z, xr)) + xr;
+		uint32_t c;
+		switch (group_level<RB>(g)) {
+		case 0: c = count_group<RB, 0>(m, g); break;
+		case 1: c = count_group<RB, 1>(m, g); break;
+		case 2: c = count_group<RB, 2>(m, g); break;
+		case 3: c = count_group<RB, 3>(m, g); break;
+		case 4: c = count_group<RB, 4>(m, g); break;
+		case 5: c = count_group<RB, 5>(m, g); break;
+		case 6: c = count_group<RB, 6>(m, g); break;
+		default: c = count_group<RB, 7>(m, g); break;
 		}
-#pragma unroll
-		for (int d = 16; d; d >>= 1) c += __shfl_xor_sync(kFull, c, d);
 		if (lane == 0) m.grp[g] = c;
 	}
 	__syncthreads();
@@ -1096,17 +1153,13 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 	int16_t *dst = (int16_t *)asvl.base + s_base * 8u;
 	const bool sh_in = shadow_window_inside<RB>(S, cv, lod_max);
 	/* pass 2: warps take the non-empty groups from a shared counter */
-	static_assert(kMaxLevels == 8, "one splat_group case per level");
 	for (;;) {
 		uint32_t k = 0;
 		if (lane == 0) k = atomicAdd(&s_next, 1u);
 		k = __shfl_sync(kFull, k, 0);
 		if (k >= listed) break;
 		const int g = m.glist[k];
-		int l = 0;
-#pragma unroll
-		for (int i = 1; i < kMaxLevels; i++) l += g >= c_lv.gstart[RB][i] ? 1 : 0;
-		switch (l) {
+		switch (group_level<RB>(g)) {
 		case 0: splat_group<RB, 0>(S, stream, m, cv, g, dst, sh_in); break;
 		case 1: splat_group<RB, 1>(S, stream, m, cv, g, dst, sh_in); break;
 		case 2: splat_group<RB, 2>(S, stream, m, cv, g, dst, sh_in); break;
