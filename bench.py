@@ -296,6 +296,20 @@ def run_ours(args):
     e2e_value = n_e2e * world.nchunks / e2e_s
     if not (used_p == used and np.array_equal(sets[(n_e2e - 1) % 2][1]["svl_total"], res_h["svl_total"])):
         raise RuntimeError("pipelined end-to-end rebuild disagrees with the synchronous one")
+    # the host link's own device->host rate for the same bytes (one pinned
+    # copy): the bound of the end-to-end step
+    link_dev = torch.empty(d2h, dtype=torch.uint8, device="cuda:%d" % dev)
+    link_host = torch.empty(d2h, dtype=torch.uint8).pin_memory()
+    link_ms = []
+    for _ in range(4):
+        a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a_.record()
+        link_host.copy_(link_dev, non_blocking=True)
+        b_.record()
+        torch.cuda.synchronize()
+        link_ms.append(a_.elapsed_time(b_))
+    link_gbs = d2h / (float(np.median(link_ms[1:])) * 1e6)
+    del link_dev, link_host
     out = {
         "metric": METRIC,
         "value": round(value, 1),
@@ -321,7 +335,10 @@ def run_ours(args):
                         "stream back per slab, and under the next step's upload and compute) -> two alternating "
                         "pinned host buffer sets + result records; clock stops after the last step's copies",
                 "synchronous": {"value": round(e2e_sync_value, 1), "unit": "chunks/s",
-                                "path": "vp_world_rebuild_to_host: each step's copies end before the next starts"}},
+                                "path": "vp_world_rebuild_to_host: each step's copies end before the next starts"},
+                "link": {"d2h_gbs": round(link_gbs, 1), "bound_ms_per_step": round(d2h / link_gbs / 1e6, 3),
+                         "frac": round((d2h / link_gbs / 1e6) / (e2e_s * 1e3 / n_e2e), 4),
+                         "note": "one pinned device->host copy of d2h_bytes_per_step, CUDA events"}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": ncu_traffic(),
                      "traffic_source": "profiles/k_geometry_config2_world.md (ncu dram__bytes_read+write.sum)",
