@@ -1281,7 +1281,7 @@ __global__ void __launch_bounds__(512, 1) k_shell_big(const SetDesc *__restrict_
 	}
 }
 
-__global__ void __launch_bounds__(512, 1) k_geometry_big(const SetDesc *__restrict__ sets,
+__global__ void __launch_bounds__(1024, 1) k_geometry_big(const SetDesc *__restrict__ sets,
 							 const WorkItem *__restrict__ items, uint32_t nitems,
 							 unsigned int *queue, ChunkOut *outs, Arena asvl, Arena avbo,
 							 Arena aibo, int lod_max, uint8_t *scratch)
@@ -1381,7 +1381,9 @@ static cudaError_t launch_big(const GeoLaunch &L, cudaStream_t st)
 	}
 	if (L.n_items) {
 		const uint32_t grid = std::min(L.n_items, L.big_slots);
-		k_geometry_big<<<grid, 512, 0, st>>>(L.sets, L.items, L.n_items, L.queue, L.outs, L.svl, L.vbo, L.ibo,
+		/* 1024 threads at 64 registers: twice the warps of the small path's
+		 * CTAs to hide the latency of the scratch, which lives in L2 */
+		k_geometry_big<<<grid, 1024, 0, st>>>(L.sets, L.items, L.n_items, L.queue, L.outs, L.svl, L.vbo, L.ibo,
 						    L.lod_max, L.big_scratch);
 		e = cudaGetLastError();
 	}
