@@ -250,6 +250,7 @@ VP_API void vp_world_destroy(vp_world *w)
 	dev_free(w->d_shell_col);
 	dev_free(w->d_big);
 	dev_free(w->d_check);
+	dev_free(w->d_dec);
 	dev_free(w->d_cull_slots);
 	dev_free(w->d_cull_blocks);
 	dev_free(w->d_cull_out);
@@ -561,6 +562,24 @@ static int ensure_items(vp_world *w)
 	return VP_OK;
 }
 
+uint8_t *vpi_decoded(vp_world *w)
+{
+	const size_t need = (size_t)w->nchunks * decoded_bytes_per_chunk(w->root_bitw);
+	if (!need || w->dec_failed) return nullptr;
+	if (w->d_dec && w->dec_bytes >= need) return w->d_dec;
+	size_t free_b = 0, total_b = 0;
+	/* keep 4 GiB free for arenas and the rest; without room, decode twice */
+	if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || free_b < need + (4ull << 30) ||
+	    cudaMalloc(&w->d_dec, need) != cudaSuccess) {
+		cudaGetLastError();
+		w->d_dec = nullptr;
+		w->dec_failed = true;
+		return nullptr;
+	}
+	w->dec_bytes = need;
+	return w->d_dec;
+}
+
 int vpi_ensure_arenas(vp_world *w)
 {
 	/* first guess: 16 KiB of each output per chunk, at least 16 MiB; an
@@ -652,6 +671,7 @@ static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 	L.threads = 512;
 	L.outs = w->d_outs;
 	L.lod_max = lod_max;
+	L.decoded = vpi_decoded(w); /* every chunk is shelled before any geometry */
 	Arena *ar[3] = {&L.svl, &L.vbo, &L.ibo};
 	for (int a = 0; a < 3; a++) {
 		ar[a]->base = w->d_arena[a];
@@ -1122,6 +1142,7 @@ static int stream_rebuild(vp_world *w, int lod_max, unsigned flags, int slabs, v
 	L.threads = 512;
 	L.outs = w->d_outs;
 	L.lod_max = lod_max;
+	L.decoded = vpi_decoded(w); /* every chunk is shelled before the slabs */
 	Arena *ar[3] = {&L.svl, &L.vbo, &L.ibo};
 	for (int a = 0; a < 3; a++) {
 		ar[a]->base = w->d_arena[a];

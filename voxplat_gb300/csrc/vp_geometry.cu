@@ -69,6 +69,9 @@ struct Geo {
 	static constexpr size_t o_sv = a16(o_e0p + sizeof(uint64_t) * 3 * R);
 	static constexpr size_t o_nbr = a16(o_sv + sizeof(uint64_t) * 2 * R);
 	static constexpr size_t bytes = a16(o_nbr + sizeof(int32_t) * 28);
+	/* a decoded chunk handed from the shell pass to the geometry pass:
+	 * occupancy rows and run-start rows (u64, row r = z R + y), then ranks */
+	static constexpr size_t dec_bytes = (size_t)RR * (8 + 8 + 4);
 	static constexpr size_t shell_words = 6 * R;   /* u64 per chunk */
 	static constexpr size_t shell_cols = 3 * RR;   /* bytes per chunk */
 };
@@ -274,13 +277,60 @@ __device__ __forceinline__ uint32_t colour_at(const uint32_t *__restrict__ s, co
 	return __ldg(s + run) >> 24;
 }
 
+/* The decoded chunk (occupancy rows without halo, run-start rows, ranks)
+ * to global memory, and back: the shell pass decodes every chunk anyway,
+ * so the geometry pass of the same rebuild loads instead of decoding. */
+template <int RB>
+__device__ void store_decoded(const Smem &m, uint8_t *dst)
+{
+	using G = Geo<RB>;
+	constexpr int R = G::R, RR = G::RR;
+	uint64_t *occ = (uint64_t *)dst;
+	uint4 *rs = (uint4 *)(dst + (size_t)RR * 8);
+	uint4 *rank = (uint4 *)(dst + (size_t)RR * 16);
+	for (int r = threadIdx.x; r < RR; r += blockDim.x) occ[r] = m.occ[hidx<RB>(r & (R - 1), r >> RB)];
+	for (int i = threadIdx.x; i < RR / 2; i += blockDim.x) rs[i] = ((const uint4 *)m.rs)[i];
+	for (int i = threadIdx.x; i < RR / 4; i += blockDim.x) rank[i] = ((const uint4 *)m.rank)[i];
+}
+
+/* 8- and 16-byte asynchronous global -> shared copies (cp.async): every
+ * thread has all of its copies in flight at once. */
+__device__ __forceinline__ void copy_async8(void *dst, const void *src)
+{
+	asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+		     "l"(src)
+		     : "memory");
+}
+
+__device__ __forceinline__ void copy_async16(void *dst, const void *src)
+{
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+		     "l"(src)
+		     : "memory");
+}
+
+template <int RB>
+__device__ void load_decoded(const uint8_t *src, const Smem &m)
+{
+	using G = Geo<RB>;
+	constexpr int R = G::R, RR = G::RR;
+	const uint64_t *occ = (const uint64_t *)src;
+	const uint4 *rs = (const uint4 *)(src + (size_t)RR * 8);
+	const uint4 *rank = (const uint4 *)(src + (size_t)RR * 16);
+	for (int r = threadIdx.x; r < RR; r += blockDim.x) copy_async8(m.occ + hidx<RB>(r & (R - 1), r >> RB), occ + r);
+	for (int i = threadIdx.x; i < RR / 2; i += blockDim.x) copy_async16((uint4 *)m.rs + i, rs + i);
+	for (int i = threadIdx.x; i < RR / 4; i += blockDim.x) copy_async16((uint4 *)m.rank + i, rank + i);
+	asm volatile("cp.async.wait_all;\n" ::: "memory");
+	__syncthreads();
+}
+
 /* ------------------------------------------------------------------ */
 /* Shell pass                                                          */
 /* ------------------------------------------------------------------ */
 
 template <int RB>
 __global__ void __launch_bounds__(512, 2) k_shell(const SetDesc *__restrict__ sets, const WorkItem *__restrict__ items,
-					       uint32_t nitems)
+					       uint32_t nitems, uint8_t *decoded)
 {
 	using G = Geo<RB>;
 	constexpr int R = G::R, RR = G::RR;
@@ -294,6 +344,7 @@ __global__ void __launch_bounds__(512, 2) k_shell(const SetDesc *__restrict__ se
 	if (chunk_is_null(S, wi.chunk, N)) return;
 	const uint32_t *stream = S.pool + S.off[wi.chunk];
 	decode_chunk<RB>(stream, S.len[wi.chunk] - 1u, m);
+	if (decoded) store_decoded<RB>(m, decoded + (size_t)wi.chunk * G::dec_bytes);
 	uint64_t *bits = S.shell_bits + (size_t)wi.chunk * G::shell_words;
 	uint8_t *cols = S.shell_col + (size_t)wi.chunk * G::shell_cols;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -1198,7 +1249,8 @@ __device__ void mask_dense(const SetDesc &S, const uint32_t *__restrict__ stream
  * mesh / splats. Returns with the block synchronised. */
 template <int RB>
 __device__ __forceinline__ void geometry_item(const SetDesc &S, const WorkItem &wi, ChunkOut *out, const Smem &m,
-					      const Arena &asvl, const Arena &avbo, const Arena &aibo, int lod_max)
+					      const Arena &asvl, const Arena &avbo, const Arena &aibo, int lod_max,
+					      const uint8_t *decoded = nullptr)
 {
 	using G = Geo<RB>;
 	constexpr int R = G::R;
@@ -1222,7 +1274,11 @@ __device__ __forceinline__ void geometry_item(const SetDesc &S, const WorkItem &
 		return;
 	}
 	const uint32_t *stream = S.pool + S.off[wi.chunk];
-	decode_chunk<RB>(stream, S.len[wi.chunk] - 1u, m);
+	/* the shell pass of this rebuild stored every chunk but the all-air ones */
+	if (decoded && !chunk_is_null(S, wi.chunk, N))
+		load_decoded<RB>(decoded + (size_t)wi.chunk * G::dec_bytes, m);
+	else
+		decode_chunk<RB>(stream, S.len[wi.chunk] - 1u, m);
 	load_halo<RB>(S, m);
 	if (wi.flags & kItemMaskDense)
 		mask_dense<RB>(S, stream, m, (uint8_t *)asvl.base + (size_t)wi.slot * G::S * G::S * G::S);
@@ -1236,7 +1292,7 @@ __device__ __forceinline__ void geometry_item(const SetDesc &S, const WorkItem &
 template <int RB>
 __global__ void __launch_bounds__(512, 2) k_geometry(const SetDesc *__restrict__ sets, const WorkItem *__restrict__ items,
 						     uint32_t nitems, unsigned int *queue, ChunkOut *outs, Arena asvl,
-						     Arena avbo, Arena aibo, int lod_max)
+						     Arena avbo, Arena aibo, int lod_max, const uint8_t *decoded)
 {
 	extern __shared__ __align__(16) uint8_t smem[];
 	const Smem m = carve<RB>(smem);
@@ -1250,7 +1306,7 @@ __global__ void __launch_bounds__(512, 2) k_geometry(const SetDesc *__restrict__
 		next = nitems;
 		const WorkItem wi = items[it];
 		const SetDesc S = sets[wi.set];
-		geometry_item<RB>(S, wi, outs + wi.slot, m, asvl, avbo, aibo, lod_max);
+		geometry_item<RB>(S, wi, outs + wi.slot, m, asvl, avbo, aibo, lod_max, decoded);
 	}
 }
 
@@ -1354,14 +1410,14 @@ static cudaError_t launch_rb(const GeoLaunch &L, cudaStream_t st)
 	e = cudaFuncSetAttribute(k_geometry<RB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::bytes);
 	if (e != cudaSuccess) return e;
 	if (L.run_shell && L.n_shell) {
-		k_shell<RB><<<L.n_shell, L.threads, G::bytes, st>>>(L.sets, L.shell_items, L.n_shell);
+		k_shell<RB><<<L.n_shell, L.threads, G::bytes, st>>>(L.sets, L.shell_items, L.n_shell, L.decoded);
 		e = cudaGetLastError();
 		if (e != cudaSuccess) return e;
 	}
 	if (L.n_items) {
 		const uint32_t grid = L.queue ? L.ctas : L.n_items;
 		k_geometry<RB><<<grid, L.threads, G::bytes, st>>>(L.sets, L.items, L.n_items, L.queue, L.outs, L.svl, L.vbo,
-								 L.ibo, L.lod_max);
+								 L.ibo, L.lod_max, L.decoded);
 		e = cudaGetLastError();
 	}
 	return e;
@@ -1470,6 +1526,11 @@ size_t shell_words_per_chunk(int root_bitw)
 	return root_bitw == 7 ? Big::shell_words : 6u * (1u << root_bitw);
 }
 size_t shell_cols_per_chunk(int root_bitw) { return 3u * (1u << root_bitw) * (1u << root_bitw); }
+
+size_t decoded_bytes_per_chunk(int root_bitw)
+{
+	return root_bitw >= 3 && root_bitw <= 6 ? (size_t)(1u << (2 * root_bitw)) * 20u : 0u;
+}
 
 cudaError_t launch_geometry(int root_bitw, const GeoLaunch &L, cudaStream_t st)
 {

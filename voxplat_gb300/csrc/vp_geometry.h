@@ -19,12 +19,18 @@ struct GeoLaunch {
 	int lod_max;
 	uint8_t *big_scratch;       /* 128^3 chunks: per-CTA working sets */
 	uint32_t big_slots;         /* slots in big_scratch = CTAs of a launch */
+	/* <= 64^3 chunks, or NULL: decoded_bytes_per_chunk() per chunk. The
+	 * shell pass stores each chunk it decodes there; the geometry pass
+	 * loads them instead of decoding, so a launch pair that passes it must
+	 * shell every non-empty chunk whose geometry it builds. */
+	uint8_t *decoded;
 };
 
 size_t geometry_smem_bytes(int root_bitw);
 size_t big_scratch_slot_bytes();
 size_t shell_words_per_chunk(int root_bitw);
 size_t shell_cols_per_chunk(int root_bitw);
+size_t decoded_bytes_per_chunk(int root_bitw);
 int geometry_ctas_per_sm(int root_bitw, int threads);
 cudaError_t launch_geometry(int root_bitw, const GeoLaunch &L, cudaStream_t st);
 /* One persistent launch over items of any root size (sets may differ in

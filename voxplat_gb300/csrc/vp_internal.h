@@ -62,6 +62,9 @@ struct vp_world {
 	uint16_t *d_shadow = nullptr;
 	uint64_t shadow_len = 0;
 	uint64_t shadow_cap = 0;                 /* elements allocated in d_shadow */
+	uint8_t *d_dec = nullptr;                /* decoded chunks, shell pass -> geometry pass */
+	size_t dec_bytes = 0;
+	bool dec_failed = false;                 /* no room: rebuilds decode twice */
 	uint32_t *d_check = nullptr;             /* upload validation: status, first bad chunk */
 	uint32_t *h_check = nullptr;             /* its mapped pinned copy, and that copy's device address */
 	uint32_t *h_check_dev = nullptr;
@@ -177,4 +180,7 @@ int vpi_world_run(vp_world *w, const WorkItem *items, uint32_t n, int lod_max);
  * voxels with nonzero run lengths. */
 /* waits for the copies of pipelined streamed rebuilds and rebases their results */
 extern "C" int vpi_pipe_drain(vp_world *w);
+/* the decoded-chunk handoff buffer of a full rebuild, or NULL (128^3 roots,
+ * or not enough free device memory: the geometry pass then decodes) */
+extern "C" uint8_t *vpi_decoded(vp_world *w);
 extern "C" int vpi_validate_stream(const uint32_t *s, uint32_t n, uint64_t N);
