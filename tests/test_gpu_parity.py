@@ -273,3 +273,38 @@ def test_pipelined_rebuilds_match_the_synchronous_one(ctx, tiny):
     bufs = [np.zeros(1 << 22, np.int16), np.zeros(1 << 22, np.int16), np.zeros(1 << 21, np.uint32)]
     dw.rebuild_to_host(3, *bufs, res, slabs=2)
     assert _same_outputs(want[3][0], want[3][1], res, bufs) is None
+
+
+def test_full_rebuilds_never_see_a_stale_decoded_handoff(ctx):
+    """Full rebuilds hand each decoded chunk from the shell pass to the
+    geometry pass. Uploading another world of the same size, edits between
+    full rebuilds, and switching between synchronous, streamed and pipelined
+    rebuilds must each leave every chunk bit-exact to the oracle."""
+    a = worlds.cave_world(5, (2, 1, 2), seed=31)
+    b = worlds.cave_world(5, (2, 1, 2), seed=32)
+    oa, ob = OracleWorld(a), OracleWorld(b)
+    modes = (np.arange(a.nchunks) % 3 == 0).astype(np.uint8)
+    dw = gpu.DeviceWorld(ctx, a)
+    assert worlds.compare_world(dw, oa, modes, 4) == []
+    dw.upload_arrays(b.pool, b.off, b.len, b.shadow, b.shadow_w)
+    assert worlds.compare_world(dw, ob, modes, 4) == []
+    dw.upload_arrays(a.pool, a.off, a.len, a.shadow, a.shadow_w)
+    assert worlds.compare_world(dw, oa, None, 3) == []
+    # edits (remeshed without the handoff), then full rebuilds of the edited world
+    edits = [(40, 30, 50, 9, 0), (70, 20, 90, 6, 77), (10, 5, 120, 12, 0)]
+    for e in edits:
+        oa.edit_sphere(e[:3], e[3], e[4])
+    dw.set_modes(modes)
+    dw.edit(gpu.make_edits(edits))
+    assert worlds.compare_world(dw, oa, modes, 4) == []
+    res = np.zeros(a.nchunks, gpu.RESULT_DTYPE)
+    bufs = [np.zeros(1 << 22, np.int16), np.zeros(1 << 22, np.int16), np.zeros(1 << 21, np.uint32)]
+    dw.rebuild_to_host_async(4, *bufs, res, slabs=3)
+    dw.outputs_wait()
+    for c in range(a.nchunks):
+        if modes[c]:
+            continue
+        n0 = int(res[c]["svl_off"])
+        got = bufs[0][n0:n0 + int(res[c]["svl_total"])]
+        assert np.array_equal(got, oa.splats(c, 4)[0]), c
+    assert worlds.compare_world(dw, oa, modes, 2) == []
