@@ -129,11 +129,13 @@ VP_API int vp_world_rebuild_to_host(vp_world *w, int lod_max, unsigned flags, in
  * are issued and the previous call's copies have finished, so rebuild k+1
  * (and the upload before it) computes while rebuild k's outputs are being
  * copied. Calls alternate between two halves of each output arena and two
- * sets of result records, and so must the caller's host buffers: those of
+ * sets of result records, and so should the caller's host buffers: those of
  * call k (and `results`, whose offsets are then rebased to the host
  * buffers) are final once call k+1 or vp_world_outputs_wait returns, or a
- * synchronous rebuild, an edit or a reserve, which wait too. used_bytes[]
- * is final on return. Outputs are identical to vp_world_rebuild_to_host's. */
+ * synchronous rebuild, an edit or a reserve, which wait too. A call given
+ * the previous call's `results` again first finishes that call (no
+ * overlap). used_bytes[] is final on return. Outputs are identical to
+ * vp_world_rebuild_to_host's. */
 VP_API int vp_world_rebuild_to_host_async(vp_world *w, int lod_max, unsigned flags, int slabs, void *svl,
 					  uint64_t svl_bytes, void *vbo, uint64_t vbo_bytes, void *ibo,
 					  uint64_t ibo_bytes, vp_chunk_result *results, uint64_t used_bytes[3]);

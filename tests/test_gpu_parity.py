@@ -308,3 +308,26 @@ def test_full_rebuilds_never_see_a_stale_decoded_handoff(ctx):
         got = bufs[0][n0:n0 + int(res[c]["svl_total"])]
         assert np.array_equal(got, oa.splats(c, 4)[0]), c
     assert worlds.compare_world(dw, oa, modes, 2) == []
+
+
+def test_pipelined_rebuilds_reusing_one_buffer_set(ctx):
+    """A caller that does not alternate buffer sets still gets each call's
+    outputs: the previous call is finished before its records are reused."""
+    w = worlds.cave_world(5, (2, 1, 2), seed=33)
+    modes = (np.arange(w.nchunks) % 5 == 2).astype(np.uint8)
+    ref = gpu.DeviceWorld(ctx, w)
+    ref.set_modes(modes)
+    want = {}
+    for lod in (2, 4):
+        res = np.zeros(w.nchunks, gpu.RESULT_DTYPE)
+        bufs = [np.zeros(1 << 22, np.int16), np.zeros(1 << 22, np.int16), np.zeros(1 << 21, np.uint32)]
+        ref.rebuild_to_host(lod, *bufs, res, slabs=2)
+        want[lod] = (res, bufs)
+    dw = gpu.DeviceWorld(ctx, w)
+    dw.set_modes(modes)
+    res = np.zeros(w.nchunks, gpu.RESULT_DTYPE)
+    bufs = [np.zeros(1 << 22, np.int16), np.zeros(1 << 22, np.int16), np.zeros(1 << 21, np.uint32)]
+    for lod in (4, 2, 4, 2):
+        dw.rebuild_to_host_async(lod, *bufs, res, slabs=3)
+    dw.outputs_wait()
+    assert _same_outputs(want[2][0], want[2][1], res, bufs) is None

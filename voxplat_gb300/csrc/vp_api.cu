@@ -1113,6 +1113,9 @@ static int stream_rebuild(vp_world *w, int lod_max, unsigned flags, int slabs, v
 		}
 		/* this half was last written two calls ago: its copies end first */
 		if ((rc = settle_half(w, h))) return rc;
+		/* a caller that passes the previous call's result records again gets
+		 * that call finished (and rebased) before they are overwritten */
+		if (w->rebase[h ^ 1].res == results && (rc = settle_half(w, h ^ 1))) return rc;
 		w->d_outs = w->outs_alt[h];
 	}
 	/* slab k takes ranks k, k + S, k + 2S, ... of the longest-first order, so
