@@ -152,16 +152,21 @@ def cpu_baseline(world, modes, budget_s=12.0, threads=None):
             "sample": "%d of the %d chunks (random, seed 1), cold decode, same modes/LOD" % (n, world.nchunks)}
 
 
-def ncu_traffic(name="k_geometry_config2_world.md"):
-    """DRAM bytes per launch of k_geometry from the committed ncu summary."""
+def profile_value(key, name="k_geometry_config2_world.md", cast=int):
+    """A `key: value` line of a committed ncu summary under profiles/."""
     try:
         with open(os.path.join(ROOT, "profiles", name)) as f:
             for line in f:
-                if line.startswith("traffic_bytes_per_launch:"):
-                    return int(line.split(":")[1])
-    except OSError:
+                if line.startswith(key + ":"):
+                    return cast(line.split(":")[1])
+    except (OSError, ValueError):
         pass
     return None
+
+
+def ncu_traffic(name="k_geometry_config2_world.md"):
+    """DRAM bytes per launch of k_geometry from the committed ncu summary."""
+    return profile_value("traffic_bytes_per_launch", name)
 
 
 def algorithmic_bytes(world, res):
@@ -346,7 +351,10 @@ def run_ours(args):
                      "algorithmic_bytes_per_launch": int(ab),
                      "bytes_split": {"rle_in": rle_b, "geometry_out": out_b, "shadow_map": sh_b},
                      "step_bytes": int(step_bytes),
-                     "step_frac": round(step_bytes / (t_ms / args.steps / 1e3) / 1e9 / peak, 4)},
+                     "step_frac": round(step_bytes / (t_ms / args.steps / 1e3) / 1e9 / peak, 4),
+                     "issue_active_frac": profile_value("issue_active_frac", cast=float),
+                     "issue_note": "the kernel is issue/latency-bound: fraction of cycles each SM sub-partition "
+                                   "issued an instruction (ncu smsp__issue_active, profiles/)"},
         "gpu_launches": int(launches),
     }
     if rank == 0:
