@@ -152,7 +152,7 @@ def cpu_baseline(world, modes, budget_s=12.0, threads=None):
             "sample": "%d of the %d chunks (random, seed 1), cold decode, same modes/LOD" % (n, world.nchunks)}
 
 
-def profile_value(key, name="k_geometry_config2_world.md", cast=int):
+def profile_value(key, name="k_geometry_world_2048x256x2048.md", cast=int):
     """A `key: value` line of a committed ncu summary under profiles/."""
     try:
         with open(os.path.join(ROOT, "profiles", name)) as f:
@@ -164,7 +164,7 @@ def profile_value(key, name="k_geometry_config2_world.md", cast=int):
     return None
 
 
-def ncu_traffic(name="k_geometry_config2_world.md"):
+def ncu_traffic(name="k_geometry_world_2048x256x2048.md"):
     """DRAM bytes per launch of k_geometry from the committed ncu summary."""
     return profile_value("traffic_bytes_per_launch", name)
 
@@ -346,7 +346,7 @@ def run_ours(args):
                          "note": "one pinned device->host copy of d2h_bytes_per_step, CUDA events"}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": ncu_traffic(),
-                     "traffic_source": "profiles/k_geometry_config2_world.md (ncu dram__bytes_read+write.sum)",
+                     "traffic_source": "profiles/k_geometry_world_2048x256x2048.md (ncu dram__bytes_read+write.sum)",
                      "kernel": "k_geometry<6>", "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": int(ab),
                      "bytes_split": {"rle_in": rle_b, "geometry_out": out_b, "shadow_map": sh_b},

@@ -62,8 +62,8 @@ def main():
     if ob.ref_lib() is None:
         sys.exit("reference tree not found; set VP_REFERENCE")
     # one 64^3 terrain chunk (heights 8..56, colour 1 + h/4 + jitter)
-    w = worlds.config1_chunk(seed=1)
-    save("config1_chunk", **world_arrays(w), **geometry(ob.RefWorld(w), w.nchunks, (3, 4)))
+    w = worlds.terrain_chunk64(seed=1)
+    save("terrain_chunk64", **world_arrays(w), **geometry(ob.RefWorld(w), w.nchunks, (3, 4)))
     # multi-chunk cave worlds: halo and shadow-map handling across chunks
     w = worlds.cave_world(5, (1, 3, 1), seed=7)
     save("caves_r32", **world_arrays(w), **geometry(ob.RefWorld(w), w.nchunks, (4,)))

@@ -17,14 +17,14 @@ def ctx():
 
 
 @pytest.mark.parametrize("lod_max", [3, 4])
-def test_config1_chunk_splats(ctx, lod_max):
-    w = worlds.config1_chunk()
+def test_terrain_chunk64_splats(ctx, lod_max):
+    w = worlds.terrain_chunk64()
     dw = gpu.DeviceWorld(ctx, w)
     assert worlds.compare_world(dw, OracleWorld(w), None, lod_max) == []
 
 
-def test_config1_chunk_mesh(ctx):
-    w = worlds.config1_chunk()
+def test_terrain_chunk64_mesh(ctx):
+    w = worlds.terrain_chunk64()
     dw = gpu.DeviceWorld(ctx, w)
     assert worlds.compare_world(dw, OracleWorld(w), np.ones(1, np.uint8), 4) == []
 

@@ -4,7 +4,7 @@ import numpy as np
 from voxplat_gb300 import worldgen as wg
 
 
-def config1_chunk(seed=1):
+def terrain_chunk64(seed=1):
     """One 64^3 terrain chunk (heights 8..56, colour 1 + h/4 + jitter)."""
     return wg.terrain(wg.TERRAIN_SMALL, 6, (0, 0, 0), seed=seed)
 
