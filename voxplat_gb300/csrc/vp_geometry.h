@@ -39,4 +39,20 @@ cudaError_t launch_geometry(int root_bitw, const GeoLaunch &L, cudaStream_t st);
 int geometry_mixed_ctas_per_sm(int min_blocks, int threads);
 cudaError_t launch_geometry_mixed(int min_blocks, const GeoLaunch &L, cudaStream_t st);
 
+/* per-translation-unit launchers behind the dispatchers above (one root size
+ * or one mixed variant per unit, so the kernels compile in parallel) */
+cudaError_t launch_geometry_r3(const GeoLaunch &L, cudaStream_t st);
+cudaError_t launch_geometry_r4(const GeoLaunch &L, cudaStream_t st);
+cudaError_t launch_geometry_r5(const GeoLaunch &L, cudaStream_t st);
+cudaError_t launch_geometry_r6(const GeoLaunch &L, cudaStream_t st);
+cudaError_t launch_big(const GeoLaunch &L, cudaStream_t st);
+int geometry_ctas_per_sm_r3(int threads);
+int geometry_ctas_per_sm_r4(int threads);
+int geometry_ctas_per_sm_r5(int threads);
+int geometry_ctas_per_sm_r6(int threads);
+int geometry_mixed_ctas_per_sm_b1(int threads);
+int geometry_mixed_ctas_per_sm_b2(int threads);
+cudaError_t launch_geometry_mixed_b1(uint32_t grid, const GeoLaunch &L, cudaStream_t st);
+cudaError_t launch_geometry_mixed_b2(uint32_t grid, const GeoLaunch &L, cudaStream_t st);
+
 } // namespace vp

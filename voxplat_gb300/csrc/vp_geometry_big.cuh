@@ -10,7 +10,7 @@
  *   - the chunk's working set (occupancy with halo, run starts, run ranks,
  *     level rows: ~660 KB) does not fit in shared memory, so each CTA owns a
  *     slot of global scratch (L2 resident while the CTA works on it).
- * Included by vp_geometry.cu after the <= 64^3 path, whose helpers it uses.
+ * Included by vp_geometry_dev.cuh after the <= 64^3 path, whose helpers it uses.
  */
 #pragma once
 
@@ -82,7 +82,7 @@ __device__ __forceinline__ int bh(int y, int z) { return ((z + 1) * Big::H + (y 
 
 /* RLE stream -> occupancy rows, run-start rows and per-row run ranks, as
  * decode_chunk with 128-bit rows (four u32 words per row for the atomics). */
-__device__ void decode_big(const uint32_t *__restrict__ s, uint32_t nruns, const BigMem &m)
+static __device__ void decode_big(const uint32_t *__restrict__ s, uint32_t nruns, const BigMem &m)
 {
 	constexpr int R = Big::R, RR = Big::RR;
 	for (int r = threadIdx.x; r < RR; r += blockDim.x) {
@@ -225,7 +225,7 @@ __device__ __forceinline__ uint32_t colour_at_big(const uint32_t *__restrict__ s
 /* Shell of a decoded 128^3 chunk: planes x = 0 / R-1 (bits over y, per z),
  * y = 0 / R-1 (rows per z), z = 0 / R-1 (rows per y), two words each, and
  * the colours of the three low planes. */
-__device__ void shell_big(const uint32_t *__restrict__ stream, const BigMem &m, uint64_t *bits, uint8_t *cols)
+static __device__ void shell_big(const uint32_t *__restrict__ stream, const BigMem &m, uint64_t *bits, uint8_t *cols)
 {
 	constexpr int R = Big::R, RR = Big::RR;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -292,7 +292,7 @@ __device__ __forceinline__ void shell_xrow_big(const SetDesc &S, int32_t nc, int
 	w1 = b[(p * R + lz) * 2 + 1];
 }
 
-__device__ void load_halo_big(const SetDesc &S, const BigMem &m)
+static __device__ void load_halo_big(const SetDesc &S, const BigMem &m)
 {
 	constexpr int R = Big::R, H = Big::H;
 	for (int i = threadIdx.x; i < 2 * H + 2 * R; i += blockDim.x) {
@@ -349,7 +349,7 @@ __device__ __forceinline__ uint32_t occ_at_big(const BigMem &m, int x, int y, in
 }
 
 /* Replace the occupancy rows by the L0 mask rows, as splat_prepare. */
-__device__ void splat_prepare_big(const BigMem &m)
+static __device__ void splat_prepare_big(const BigMem &m)
 {
 	constexpr int R = Big::R;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -520,7 +520,7 @@ __device__ __forceinline__ void emit_splat_big(const SetDesc &S, const uint32_t 
 	store_splat(dst, wx, wy, wz, colour | (shadow << 6));
 }
 
-__device__ void splat_chunk_big(const SetDesc &S, const uint32_t *__restrict__ stream, const BigMem &m,
+static __device__ void splat_chunk_big(const SetDesc &S, const uint32_t *__restrict__ stream, const BigMem &m,
 				const uint32_t cv[3], int lod_max, ChunkOut *out, const Arena &asvl)
 {
 	constexpr int R = Big::R;
@@ -670,7 +670,7 @@ __device__ __forceinline__ void face_bits_big(const BigMem &m, int y, int z, uin
 	f[5] = o1 ^ zp[1];
 }
 
-__device__ void mesh_chunk_big(const SetDesc &S, const uint32_t *__restrict__ stream, const BigMem &m,
+static __device__ void mesh_chunk_big(const SetDesc &S, const uint32_t *__restrict__ stream, const BigMem &m,
 			       const uint32_t cv[3], ChunkOut *out, const Arena &avbo, const Arena &aibo)
 {
 	constexpr int R = Big::R, RR = Big::RR, NG = RR / 32;
@@ -752,7 +752,7 @@ __device__ void mesh_chunk_big(const SetDesc &S, const uint32_t *__restrict__ st
 }
 
 /* The dense L0 mask of chunk_make_mask for a 128^3 chunk. */
-__device__ void mask_dense_big(const SetDesc &S, const uint32_t *__restrict__ stream, const BigMem &m, uint8_t *dst)
+static __device__ void mask_dense_big(const SetDesc &S, const uint32_t *__restrict__ stream, const BigMem &m, uint8_t *dst)
 {
 	constexpr int R = Big::R, S1 = R + 1;
 	splat_prepare_big(m);
@@ -775,7 +775,7 @@ __device__ void mask_dense_big(const SetDesc &S, const uint32_t *__restrict__ st
 }
 
 /* One 128^3 work item: decode, halo, then mask / mesh / splats. */
-__device__ void geometry_item_big(const SetDesc &S, const WorkItem &wi, ChunkOut *out, const BigMem &m,
+static __device__ void geometry_item_big(const SetDesc &S, const WorkItem &wi, ChunkOut *out, const BigMem &m,
 				  const Arena &asvl, const Arena &avbo, const Arena &aibo, int lod_max)
 {
 	constexpr int R = Big::R;
