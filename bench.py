@@ -126,17 +126,69 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def bind_near_gpu(dev):
+    """Pin this process to the CPU cores next to GPU `dev` (its PCI
+    device's local_cpulist) before any pinned host buffer is allocated, so
+    those pages land on the GPU's own NUMA node and host<->device copies do
+    not cross the socket link. Returns what was done, for the JSON line."""
+    try:
+        import torch
+        p = torch.cuda.get_device_properties(dev)
+        bus = "%04x:%02x:%02x.0" % (getattr(p, "pci_domain_id", 0), p.pci_bus_id, p.pci_device_id)
+        base = "/sys/bus/pci/devices/" + bus
+        with open(base + "/local_cpulist") as f:
+            spec = f.read().strip()
+        cpus = set()
+        for part in spec.split(","):
+            a, _, b = part.partition("-")
+            cpus.update(range(int(a), int(b or a) + 1))
+        cpus &= os.sched_getaffinity(0)
+        node = None
+        try:
+            with open(base + "/numa_node") as f:
+                node = int(f.read().strip())
+        except (OSError, ValueError):
+            pass
+        if cpus:
+            os.sched_setaffinity(0, cpus)
+        return {"pci": bus, "numa_node": node, "cpus": len(cpus)}
+    except Exception as e:  # no sysfs entry (containers, other platforms): leave affinity alone
+        return {"unbound": type(e).__name__}
+
+
 def dist_setup():
     from voxplat_gb300 import replicas
     return replicas.init("nccl")
 
 
-def cpu_baseline(world, modes, budget_s=12.0, threads=None):
-    """The oracle (C restatement of the reference mesher) on a bounded sample
-    of the workload's chunks, OpenMP over all host cores."""
+def port_calibration():
+    """oracle/port_vs_reference.json: the port's speed over the reference's
+    own C on the same chunks, threads and flags (oracle/calibrate.py)."""
+    try:
+        with open(os.path.join(ROOT, "oracle", "port_vs_reference.json")) as f:
+            c = json.load(f)
+        return {"port_vs_reference": c["port_vs_reference"], "threads": c["threads"], "cpu": c["cpu"],
+                "machine": c["machine"]}
+    except (OSError, ValueError, KeyError):
+        return None
+
+
+def cpu_baseline(world, modes, budget_s=12.0, threads=None, check=None):
+    """The cpu_baseline leg: the oracle (C restatement of the reference
+    mesher) timed on a bounded sample of the workload's chunks, OpenMP over
+    all host cores; and, as the checker, every chunk of one GPU step's
+    outputs (`check` = host svl, vbo, ibo arrays and result records)
+    compared with the oracle byte for byte."""
     from oracle.bindings import OracleWorld
-    threads = threads or os.cpu_count()
+    threads = threads or len(os.sched_getaffinity(0))
     o = OracleWorld(world)
+    parity = None
+    if check is not None:
+        t0 = time.perf_counter()
+        bad, nbad = o.check(np.arange(world.nchunks), modes, LOD_MAX, *check, nthreads=threads)
+        parity = {"checked": int(world.nchunks), "mismatches": nbad, "first_bad": bad[:8],
+                  "what": "every chunk of the last end-to-end step's host outputs vs the oracle, byte for byte",
+                  "s": round(time.perf_counter() - t0, 2)}
     rng = np.random.default_rng(1)
     order = rng.permutation(world.nchunks).astype(np.uint32)
     n = 256
@@ -148,8 +200,12 @@ def cpu_baseline(world, modes, budget_s=12.0, threads=None):
     t0 = time.perf_counter()
     o.rebuild(order[:n], modes, LOD_MAX, threads)
     dt = time.perf_counter() - t0
-    return {"value": round(n / dt, 1), "unit": "chunks/s", "cores": threads, "kind": "port",
-            "sample": "%d of the %d chunks (random, seed 1), cold decode, same modes/LOD" % (n, world.nchunks)}
+    out = {"value": round(n / dt, 1), "unit": "chunks/s", "cores": threads, "kind": "port",
+           "sample": "%d of the %d chunks (random, seed 1), cold decode, same modes/LOD" % (n, world.nchunks)}
+    cal = port_calibration()
+    if cal:
+        out["calibration"] = cal
+    return out, parity
 
 
 def profile_value(key, name="k_geometry_world_2048x256x2048.md", cast=int):
@@ -184,6 +240,8 @@ def run_ours(args):
     rank, ws, dist = dist_setup()
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
+    all_cpus = os.sched_getaffinity(0)
+    host_binding = bind_near_gpu(dev)
     world = make_world()
     modes = mesh_modes(world)
     ctx = gpu.Context(dev)
@@ -315,6 +373,7 @@ def run_ours(args):
         link_ms.append(a_.elapsed_time(b_))
     link_gbs = d2h / (float(np.median(link_ms[1:])) * 1e6)
     del link_dev, link_host
+    e2e_ms = e2e_s * 1e3 / n_e2e
     out = {
         "metric": METRIC,
         "value": round(value, 1),
@@ -329,45 +388,56 @@ def run_ours(args):
         "dtype": "u8",
         "data": "synthetic (seeded integer-hash terrain + caves; no dataset)",
         "config": workload_config(world, modes),
-        "voxels_per_s": round(value * world.R ** 3, 1),
+        "e2e": {"value": round(e2e_value, 1), "unit": "chunks/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 3),
+                "path": "pinned host world -> vp_world_upload -> vp_world_rebuild_to_host_async -> pinned host",
+                "sync_value": round(e2e_sync_value, 1),
+                "link_d2h_gbs": round(link_gbs, 1),
+                "link_bound_ms": round(d2h / link_gbs / 1e6, 3),
+                "link_frac": round((d2h / link_gbs / 1e6) / e2e_ms, 4),
+                "host": host_binding},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": ncu_traffic(), "kernel": "k_geometry<6>",
+                     "peak_source": peak_kind, "algorithmic_bytes": int(ab),
+                     "step_frac": round(step_bytes / (t_ms / args.steps / 1e3) / 1e9 / peak, 4)},
         "kernel_ms": {"shell": round(shell_ms / args.steps, 4), "geometry": round(geo_avg_ms, 4),
                       "group": round(grp_ms / args.steps, 4)},
-        "plain": {"value": round(plain_value, 1), "unit": "chunks/s", "launches_per_step": 2 * world.nchunks,
-                  "batched_over_plain": round(value / plain_value, 2)},
-        "e2e": {"value": round(e2e_value, 1), "unit": "chunks/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "steps": n_e2e, "ms_per_step": round(e2e_s * 1e3 / n_e2e, 3),
-                "path": "pinned host world -> vp_world_upload -> vp_world_rebuild_to_host_async (group; outputs "
-                        "stream back per slab, and under the next step's upload and compute) -> two alternating "
-                        "pinned host buffer sets + result records; clock stops after the last step's copies",
-                "synchronous": {"value": round(e2e_sync_value, 1), "unit": "chunks/s",
-                                "path": "vp_world_rebuild_to_host: each step's copies end before the next starts"},
-                "link": {"d2h_gbs": round(link_gbs, 1), "bound_ms_per_step": round(d2h / link_gbs / 1e6, 3),
-                         "frac": round((d2h / link_gbs / 1e6) / (e2e_s * 1e3 / n_e2e), 4),
-                         "note": "one pinned device->host copy of d2h_bytes_per_step, CUDA events"}},
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": ncu_traffic(),
-                     "traffic_source": "profiles/k_geometry_world_2048x256x2048.md (ncu dram__bytes_read+write.sum)",
-                     "kernel": "k_geometry<6>", "peak_source": peak_kind,
-                     "algorithmic_bytes_per_launch": int(ab),
-                     "bytes_split": {"rle_in": rle_b, "geometry_out": out_b, "shadow_map": sh_b},
-                     "step_bytes": int(step_bytes),
-                     "step_frac": round(step_bytes / (t_ms / args.steps / 1e3) / 1e9 / peak, 4),
-                     "issue_active_frac": profile_value("issue_active_frac", cast=float),
-                     "issue_note": "the kernel is issue/latency-bound: fraction of cycles each SM sub-partition "
-                                   "issued an instruction (ncu smsp__issue_active, profiles/)"},
+        "plain_value": round(plain_value, 1),
         "gpu_launches": int(launches),
     }
+    detail = {"detail": "bench.py sub-benchmarks; the headline is the next line",
+              "voxels_per_s": round(value * world.R ** 3, 1),
+              "plain": {"value": round(plain_value, 1), "unit": "chunks/s", "launches_per_step": 2 * world.nchunks,
+                        "batched_over_plain": round(value / plain_value, 2)},
+              "e2e": {"steps": n_e2e, "ms_per_step": round(e2e_ms, 3),
+                      "path": "pinned host world -> vp_world_upload -> vp_world_rebuild_to_host_async (group; "
+                              "outputs stream back per slab, and under the next step's upload and compute) -> two "
+                              "alternating pinned host buffer sets + result records; clock stops after the last "
+                              "step's copies",
+                      "synchronous": {"value": round(e2e_sync_value, 1), "unit": "chunks/s",
+                                      "path": "vp_world_rebuild_to_host: each step's copies end before the next"},
+                      "link": {"d2h_gbs": round(link_gbs, 1), "bound_ms_per_step": round(d2h / link_gbs / 1e6, 3),
+                               "note": "one pinned device->host copy of d2h_bytes_per_step, CUDA events"}},
+              "roofline": {"traffic_source": "profiles/k_geometry_world_2048x256x2048.md (ncu dram__bytes_read+"
+                                             "write.sum)",
+                           "bytes_split": {"rle_in": rle_b, "geometry_out": out_b, "shadow_map": sh_b},
+                           "step_bytes": int(step_bytes),
+                           "issue_active_frac": profile_value("issue_active_frac", cast=float)}}
     if rank == 0:
         out["clocks"] = clk.summary()
-        out["picking"] = picking(dw)
+        detail["picking"] = picking(dw)
         dw.rebuild(LOD_MAX, group=True)
         dw.finish()
-        out["render"] = render_frame(dw, CAMERA)
+        detail["render"] = render_frame(dw, CAMERA)
         dw.close()
         if not args.skip_edits:
-            out["edit_serving"] = edit_serving(ctx)
+            es = edit_serving(ctx)
+            detail["edit_serving"] = es
+            out["edit_p99_ms"] = es["p99_ms"]
         if not args.skip_uneven:
-            out["uneven_batch"] = uneven_batch(ctx)
+            ub = uneven_batch(ctx)
+            detail["uneven_batch"] = ub
+            out["uneven_batched_over_plain"] = ub["batched_over_plain"]
         if not args.skip_full_scale:
             fs = full_scale(ctx)
             res5, dw5 = fs.pop("_res"), fs.pop("_dw")
@@ -383,8 +453,13 @@ def run_ours(args):
             fs["step_frac_of_measured_hbm"] = round(fs["step_gbs"] / peaks()[0], 4)
             fs["draw_cull"] = draw_cull(dw5)
             dw5.close()
-            out["full_scale"] = fs
-        out["cpu_baseline"] = cpu_baseline(world, modes)
+            detail["full_scale"] = fs
+            out["full_scale_frac"] = fs["step_frac_of_measured_hbm"]
+        last = sets[(n_e2e - 1) % 2]
+        os.sched_setaffinity(0, all_cpus)  # the CPU baseline gets every host core
+        out["cpu_baseline"], out["parity"] = cpu_baseline(world, modes, check=(last[0][0], last[0][1], last[0][2],
+                                                                                last[1]))
+        print(json.dumps(detail), flush=True)
         print(json.dumps(out), flush=True)
     replicas.finish(dist)
 
@@ -632,7 +707,7 @@ def run_reference(args):
     if rank != 0:
         return
     from oracle.bindings import OracleWorld
-    threads = os.cpu_count()
+    threads = len(os.sched_getaffinity(0))
     world = make_world()
     modes = mesh_modes(world)
     o = OracleWorld(world)
@@ -664,8 +739,8 @@ def run_reference(args):
         "dtype": "u8",
         "data": "synthetic (seeded integer-hash terrain + caves; no dataset)",
         "config": workload_config(world, modes),
-        "cpu_baseline": {"value": round(value, 1), "unit": "chunks/s", "cores": threads, "kind": "port",
-                         "sample": sample},
+        "cpu_baseline": dict({"value": round(value, 1), "unit": "chunks/s", "cores": threads, "kind": "port",
+                              "sample": sample}, **({"calibration": port_calibration()} if port_calibration() else {})),
         "e2e": {"value": round(value, 1), "unit": "chunks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)

@@ -221,23 +221,32 @@ VP_API int vp_rle_decode(vp_ctx *ctx, const uint32_t *words, uint32_t nwords, ui
  * memory when they need geometry: a render or input thread that must not
  * stall on cudaMalloc's implicit device synchronisation, or an engine whose
  * own allocator owns all device memory. Every input and output is a device
- * pointer the caller provides: the chunks' RLE streams laid out as
- * vp_world_upload lays them out (each stream 16-byte aligned, at least 8
- * readable words after the last), their word offsets and lengths, the
- * shadow map, optional per-chunk mesh flags, three output buffers (splats,
- * vertices, indices; bytes) and one result record per chunk. The working
- * data lives in a fixed 4 MiB device array the library holds on every GPU
- * that loads it (enough for 256 chunks of 64^3 or 1024 of 32^3); larger
- * sets return VP_EOVERFLOW. The first call on a device looks the array up
- * (cudaGetSymbolAddress) and should come before any stream capture. Calls
- * share that array: each call resets it, and calls that overlap on the GPU
- * race. The work is queued on `stream` (asynchronous); a result whose status
- * is nonzero means an output buffer was too small for that chunk. */
+ * pointer the caller provides: the chunks' RLE streams in `pool` (4-byte
+ * aligned, pool_words readable words), their word offsets and lengths
+ * (terminator included), the shadow map, optional per-chunk mesh flags,
+ * three output buffers (splats, vertices, indices; bytes) and one result
+ * record per chunk. Streams are laid out as vp_world_upload lays them out:
+ * each starts on a 16-byte boundary and the pool holds at least 8 words
+ * after each stream's terminator. They are checked on the device before
+ * anything decodes them; a chunk whose stream is out of bounds, misaligned
+ * or malformed (a zero count, counts not summing to the chunk's voxels, no
+ * terminator) is built as air, its neighbours see air, and its result gets
+ * status VP_STATUS_BAD_STREAM. The working data lives in a fixed 4 MiB
+ * device array the library holds on every GPU that loads it (enough for 256
+ * chunks of 64^3, 512 of 32^3, 2048 of 16^3 or 4096 of 8^3); larger sets
+ * return VP_EOVERFLOW, more than 2^24 chunks VP_EUNSUPPORTED. The first call on a device looks the
+ * array up (cudaGetSymbolAddress) and should come before any stream capture.
+ * Calls share that array: each call resets it, and calls that overlap on the
+ * GPU race. The work is queued on `stream` (asynchronous); a result whose
+ * status is VP_STATUS_OVERFLOW means an output buffer was too small for
+ * that chunk. */
+#define VP_STATUS_OVERFLOW 1u   /* vp_chunk_result.status: output arena too small */
+#define VP_STATUS_BAD_STREAM 2u /* vp_chunk_result.status: the chunk's stream failed the check */
 VP_API int vp_rebuild_noalloc(int device, void *stream, int root_bitw, const int max_bitw[3], const uint32_t *pool,
-			      const uint64_t *off, const uint32_t *len, const uint16_t *shadow, uint64_t shadow_len,
-			      uint32_t shadow_w, const uint8_t *make_mesh, int lod_max, int16_t *svl, uint64_t svl_bytes,
-			      int16_t *vbo, uint64_t vbo_bytes, uint32_t *ibo, uint64_t ibo_bytes,
-			      vp_chunk_result *results);
+			      uint64_t pool_words, const uint64_t *off, const uint32_t *len, const uint16_t *shadow,
+			      uint64_t shadow_len, uint32_t shadow_w, const uint8_t *make_mesh, int lod_max,
+			      int16_t *svl, uint64_t svl_bytes, int16_t *vbo, uint64_t vbo_bytes, uint32_t *ibo,
+			      uint64_t ibo_bytes, vp_chunk_result *results);
 
 /* Draw culling and LOD selection of the last rebuild made with
  * VP_REBUILD_GROUP (octree_cull, src/game.c:319-395, started from LOD

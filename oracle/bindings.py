@@ -52,6 +52,11 @@ def vpo_lib():
         lib.vpo_octree_cull.restype = ctypes.c_uint64
         lib.vpo_octree_cull.argtypes = [ctypes.c_int, V, V, V, ctypes.c_int, V, V, V, V, V, V]
         lib.vpo_mesh_flags.argtypes = [ctypes.c_int, V, V, V]
+        lib.vpo_world_set_pool.argtypes = [V, V, V, V]
+        lib.vpo_check_chunks.restype = ctypes.c_uint32
+        lib.vpo_check_chunks.argtypes = [V, V, ctypes.c_uint32, V, ctypes.c_int, ctypes.c_int,
+                                         V, ctypes.c_uint64, V, ctypes.c_uint64, V, ctypes.c_uint64,
+                                         V, V, V, V, V, V, V, V, ctypes.c_uint32]
         _vpo = lib
     return _vpo
 
@@ -81,6 +86,8 @@ def ref_lib():
         lib.vpref_rle_compress.argtypes = [V, ctypes.c_uint32, V]
         lib.vpref_rle_decompress.restype = ctypes.c_uint32
         lib.vpref_rle_decompress.argtypes = [V, V, ctypes.c_uint32]
+        lib.vpref_rebuild.restype = ctypes.c_uint64
+        lib.vpref_rebuild.argtypes = [V, V, ctypes.c_uint32, V, ctypes.c_int, ctypes.c_int]
         _ref = lib
     return _ref
 
@@ -133,10 +140,31 @@ class OracleWorld(_Base):
         mb = (ctypes.c_int * 3)(*world.max_bitw)
         self.h = lib.vpo_world_new(world.root_bitw, mb, world.pad_rows)
         self.nchunks = world.nchunks
-        for c in range(world.nchunks):
-            s = np.ascontiguousarray(world.chunk_rle(c))
-            lib.vpo_world_set_rle(self.h, c, _vp(s), len(s))
-        lib.vpo_world_set_shadow(self.h, _vp(world.shadow), len(world.shadow))
+        pool = np.ascontiguousarray(world.pool, np.uint32)
+        off = np.ascontiguousarray(world.off, np.uint64)
+        lens = np.ascontiguousarray(world.len, np.uint32)
+        lib.vpo_world_set_pool(self.h, _vp(pool), _vp(off), _vp(lens))
+        sh = np.ascontiguousarray(world.shadow, np.uint16)
+        lib.vpo_world_set_shadow(self.h, _vp(sh), len(sh))
+
+    @classmethod
+    def partial(cls, root_bitw, max_bitw, pad_rows, streams, shadow):
+        """A world of which only some chunks are known: `streams` maps chunk
+        index -> RLE stream, every other chunk is air. Enough to check the
+        chunks whose neighbourhoods (26 neighbours) are all in `streams`."""
+        self = cls.__new__(cls)
+        lib = vpo_lib()
+        self.lib = lib
+        self.R = 1 << root_bitw
+        mb = (ctypes.c_int * 3)(*max_bitw)
+        self.h = lib.vpo_world_new(root_bitw, mb, pad_rows)
+        self.nchunks = 1 << sum(max_bitw)
+        for c, st in streams.items():
+            st = np.ascontiguousarray(st, np.uint32)
+            lib.vpo_world_set_rle(self.h, int(c), _vp(st), len(st))
+        sh = np.ascontiguousarray(shadow, np.uint16)
+        lib.vpo_world_set_shadow(self.h, _vp(sh), len(sh))
+        return self
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -169,6 +197,39 @@ class OracleWorld(_Base):
             self.lib.vpo_world_drop_voxels(self.h)
         return self.lib.vpo_rebuild(self.h, _vp(chunks), len(chunks), _vp(mm) if mm is not None else None,
                                     lod_max, nthreads)
+
+    def check(self, chunks, make_mesh, lod_max, svl, vbo, ibo, results, nthreads=None, bad_cap=64):
+        """Parity check of a candidate rebuild: `results` is a structured
+        array indexed by chunk (fields svl_off, svl_items[8], vbo_off,
+        vbo_items, ibo_off, ibo_items, status; offsets in elements of the
+        int16 svl / int16 vbo / uint32 ibo arrays). Every chunk in `chunks`
+        is recomputed (OpenMP) and compared byte for byte. Returns the list
+        of mismatching chunks (at most bad_cap of them) and their count."""
+        import os
+        nthreads = nthreads or os.cpu_count() or 1
+        chunks = np.ascontiguousarray(chunks, np.uint32)
+        mm = None if make_mesh is None else np.ascontiguousarray(make_mesh, np.uint8)
+        svl = np.ascontiguousarray(svl, np.int16)
+        vbo = np.ascontiguousarray(vbo, np.int16)
+        ibo = np.ascontiguousarray(ibo, np.uint32)
+        f = {k: np.ascontiguousarray(results[k]) for k in ("svl_off", "vbo_off", "ibo_off")}
+        f["svl_items"] = np.ascontiguousarray(results["svl_items"], np.uint32).reshape(-1)
+        assert f["svl_items"].size == 8 * len(results)
+        for k in ("vbo_items", "ibo_items", "status"):
+            f[k] = np.ascontiguousarray(results[k], np.uint32)
+        for k in ("svl_off", "vbo_off", "ibo_off"):
+            f[k] = f[k].astype(np.uint64)
+        bad = np.zeros(bad_cap, np.uint32)
+        nbad = self.lib.vpo_check_chunks(
+            self.h, _vp(chunks), len(chunks), _vp(mm) if mm is not None else None, lod_max, nthreads,
+            _vp(svl), len(svl), _vp(vbo), len(vbo), _vp(ibo), len(ibo), _vp(f["svl_off"]), _vp(f["svl_items"]),
+            _vp(f["vbo_off"]), _vp(f["vbo_items"]), _vp(f["ibo_off"]), _vp(f["ibo_items"]), _vp(f["status"]),
+            _vp(bad), bad_cap)
+        return sorted(int(b) for b in bad[:min(nbad, bad_cap)]), int(nbad)
+
+    def drop_voxels(self):
+        """Free every decoded chunk (they are decoded again on demand)."""
+        self.lib.vpo_world_drop_voxels(self.h)
 
     def group_node(self, lod, node, svl_lists, svl_items):
         """gfx_update_svl's concatenation for one node (oracle/vpo.c)."""
@@ -223,6 +284,13 @@ class RefWorld(_Base):
 
     def _splats(self, c, lod_max, geom, items, mask, work):
         return self.lib.vpref_chunk_splats(self.h, c, lod_max, _vp(geom), _vp(items), _vp(mask), _vp(work))
+
+    def rebuild(self, chunks, make_mesh, lod_max, nthreads):
+        """Timed CPU baseline on the reference's own code (cold decode)."""
+        chunks = np.ascontiguousarray(chunks, np.uint32)
+        mm = None if make_mesh is None else np.ascontiguousarray(make_mesh, np.uint8)
+        return self.lib.vpref_rebuild(self.h, _vp(chunks), len(chunks), _vp(mm) if mm is not None else None,
+                                      lod_max, nthreads)
 
     def _mesh(self, c, vbo, nv, ibo, ni):
         self.lib.vpref_chunk_mesh(self.h, c, _vp(vbo), _vp(nv), _vp(ibo), _vp(ni))

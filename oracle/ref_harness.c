@@ -29,6 +29,7 @@
 #include "chunkset/mesher.h"
 #include "chunkset/rle.h"
 
+#include <omp.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -177,4 +178,69 @@ uint32_t vpref_rle_decompress(const uint32_t *words, uint8_t *out, uint32_t n)
 	memcpy(out, v, n);
 	free(v);
 	return n;
+}
+
+/* Timed CPU baseline on the reference's own code: chunkset_manage's
+ * per-chunk work (src/chunkset.c:251-459) for a list of chunks, OpenMP over
+ * chunks like the reference (there: 4 threads, 8 chunks per 5 ms tick, a
+ * 100 ms rate limit; here: `nthreads` threads and no throttles). Cold: the
+ * decoded voxels of every chunk are dropped first, as chunk_compress leaves
+ * idle chunks (src/chunkset.c:213-230), so each chunk_open_ro decodes from
+ * RLE. Each chunk's output is copied into an exact-size buffer, as the
+ * reference publishes it (src/chunkset.c:347-358, 472-480). Returns the
+ * output bytes produced. */
+uint64_t vpref_rebuild(struct ChunkSet *set, const uint32_t *chunks, uint32_t n, const uint8_t *make_mesh,
+		       int lod_max, int nthreads)
+{
+	for (uint32_t c = 0; c < set->count; c++) {
+		struct ChunkMD *m = &set->chunks[c];
+		if (m->voxels && m->voxels != set->null_chunk->voxels && m->rle) {
+			free(m->voxels);
+			m->voxels = NULL;
+		}
+	}
+	prime_rle(set);
+	const size_t R = set->root, S3 = (R + 1) * (R + 1) * (R + 1);
+	size_t geom_cap = 16;
+	for (int l = 0; l <= lod_max; l++) geom_cap += 4 * (((R >> l) + 1) * ((R >> l) + 1) * ((R >> l) + 1));
+	uint64_t total = 0;
+#pragma omp parallel num_threads(nthreads) reduction(+ : total)
+	{
+		int16_t *geom = NULL, *vbo = NULL;
+		uint32_t *ibo = NULL;
+		uint8_t *mask = (uint8_t *)malloc(S3), *work = (uint8_t *)malloc(S3);
+#pragma omp for schedule(dynamic, 1)
+		for (uint32_t k = 0; k < n; k++) {
+			const uint32_t c = chunks[k];
+			if (make_mesh && make_mesh[c]) {
+				if (!vbo) {
+					vbo = (int16_t *)malloc(3 * R * R * R * 16 * sizeof(int16_t));
+					ibo = (uint32_t *)malloc(3 * R * R * R * 6 * sizeof(uint32_t));
+				}
+				uint32_t nv = 0, ni = 0;
+				vpref_chunk_mesh(set, c, vbo, &nv, ibo, &ni);
+				int16_t *pv = (int16_t *)malloc((size_t)nv * sizeof(int16_t) + 1);
+				uint32_t *pi = (uint32_t *)malloc((size_t)ni * sizeof(uint32_t) + 1);
+				memcpy(pv, vbo, (size_t)nv * sizeof(int16_t));
+				memcpy(pi, ibo, (size_t)ni * sizeof(uint32_t));
+				total += (uint64_t)nv * 2 + (uint64_t)ni * 4;
+				free(pv);
+				free(pi);
+			} else {
+				if (!geom) geom = (int16_t *)malloc(geom_cap * sizeof(int16_t));
+				uint32_t items[8];
+				const uint32_t t = vpref_chunk_splats(set, c, lod_max, geom, items, mask, work);
+				int16_t *ps = (int16_t *)malloc((size_t)t * sizeof(int16_t) + 1);
+				memcpy(ps, geom, (size_t)t * sizeof(int16_t));
+				total += (uint64_t)t * 2;
+				free(ps);
+			}
+		}
+		free(geom);
+		free(vbo);
+		free(ibo);
+		free(mask);
+		free(work);
+	}
+	return total;
 }

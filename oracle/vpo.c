@@ -589,6 +589,77 @@ uint64_t vpo_rebuild(vpo_world *w, const uint32_t *chunks, uint32_t n, const uin
 	return total;
 }
 
+/* Bulk form of vpo_world_set_rle for every chunk: chunk c's stream is
+ * pool[off[c] .. off[c] + len[c]). */
+void vpo_world_set_pool(vpo_world *w, const uint32_t *pool, const uint64_t *off, const uint32_t *len)
+{
+	for (uint32_t c = 0; c < w->nchunks; c++) vpo_world_set_rle(w, c, pool + off[c], len[c]);
+}
+
+/* Parity check of a candidate rebuild (the checker of the tests): for each
+ * of the n chunks in `chunks`, OpenMP over chunks, run the same per-chunk
+ * sequence as vpo_rebuild (the reference's src/chunkset.c:337-459: mesh, or
+ * mask + L0 splats + downsample/splat per level) and compare with the
+ * candidate's output of chunk c: svl[svl_off[c] ..] with per-level counts
+ * svl_items[c * 8 + l] (int16 items), or vbo[vbo_off[c] ..] / ibo[ibo_off[c]
+ * ..] with vbo_items[c] / ibo_items[c]. A chunk whose status[c] is nonzero,
+ * whose ranges fall outside the given arrays, or whose bytes differ is a
+ * mismatch. Returns the number of mismatching chunks; the first bad_cap of
+ * them (in no particular order) go to bad[]. */
+uint32_t vpo_check_chunks(vpo_world *w, const uint32_t *chunks, uint32_t n, const uint8_t *make_mesh, int lod_max,
+			  int nthreads, const int16_t *svl, uint64_t svl_len, const int16_t *vbo, uint64_t vbo_len,
+			  const uint32_t *ibo, uint64_t ibo_len, const uint64_t *svl_off, const uint32_t *svl_items,
+			  const uint64_t *vbo_off, const uint32_t *vbo_items, const uint64_t *ibo_off,
+			  const uint32_t *ibo_items, const uint32_t *status, uint32_t *bad, uint32_t bad_cap)
+{
+	const size_t R = (size_t)w->R, S3 = (R + 1) * (R + 1) * (R + 1);
+	size_t geom_cap = 16;
+	for (int l = 0; l <= lod_max; l++) geom_cap += 4 * (((R >> l) + 1) * ((R >> l) + 1) * ((R >> l) + 1));
+	uint32_t nbad = 0;
+#pragma omp parallel num_threads(nthreads)
+	{
+		int16_t *geom = NULL, *v = NULL;
+		uint32_t *ix = NULL;
+		uint8_t *mask = (uint8_t *)malloc(S3), *work = (uint8_t *)malloc(S3);
+#pragma omp for schedule(dynamic, 1)
+		for (uint32_t k = 0; k < n; k++) {
+			const uint32_t c = chunks[k];
+			int ok = status[c] == 0;
+			if (ok && make_mesh && make_mesh[c]) {
+				if (!v) {
+					v = (int16_t *)malloc(3 * R * R * R * 16 * sizeof(int16_t));
+					ix = (uint32_t *)malloc(3 * R * R * R * 6 * sizeof(uint32_t));
+				}
+				uint32_t nv = 0, ni = 0;
+				vpo_make_mesh(w, c, v, &nv, ix, &ni);
+				ok = nv == vbo_items[c] && ni == ibo_items[c] && vbo_off[c] + nv <= vbo_len &&
+				     ibo_off[c] + ni <= ibo_len &&
+				     !memcmp(vbo + vbo_off[c], v, (size_t)nv * sizeof(int16_t)) &&
+				     !memcmp(ibo + ibo_off[c], ix, (size_t)ni * sizeof(uint32_t));
+			} else if (ok) {
+				if (!geom) geom = (int16_t *)malloc(geom_cap * sizeof(int16_t));
+				uint32_t items[VPO_MAX_LEVELS];
+				const uint32_t t = vpo_chunk_splats(w, c, lod_max, geom, items, mask, work);
+				for (int l = 0; l <= lod_max; l++) ok &= items[l] == svl_items[(size_t)c * 8 + l];
+				ok = ok && svl_off[c] + t <= svl_len &&
+				     !memcmp(svl + svl_off[c], geom, (size_t)t * sizeof(int16_t));
+			}
+			if (!ok) {
+				uint32_t slot;
+#pragma omp atomic capture
+				slot = nbad++;
+				if (slot < bad_cap) bad[slot] = c;
+			}
+		}
+		free(geom);
+		free(v);
+		free(ix);
+		free(mask);
+		free(work);
+	}
+	return nbad;
+}
+
 /* ------------------------------------------------------------------ */
 /* Draw culling and LOD selection                                      */
 /* ------------------------------------------------------------------ */

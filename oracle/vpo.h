@@ -134,6 +134,16 @@ void vpo_draw_mesh(const vpo_camera *cam, const int16_t *vbo, const uint32_t *ib
 void vpo_mesh_flags(int root_bitw, const int max_bitw[3], const float *origin, uint8_t *make_mesh);
 uint64_t vpo_rebuild(vpo_world *w, const uint32_t *chunks, uint32_t n, const uint8_t *make_mesh, int lod_max,
 		     int nthreads);
+/* every chunk's stream at once: chunk c = pool[off[c] .. off[c] + len[c]) */
+void vpo_world_set_pool(vpo_world *w, const uint32_t *pool, const uint64_t *off, const uint32_t *len);
+/* Parity check of a candidate rebuild's outputs against vpo_rebuild's
+ * per-chunk sequence, OpenMP over the listed chunks; returns the number of
+ * mismatching chunks and lists up to bad_cap of them. */
+uint32_t vpo_check_chunks(vpo_world *w, const uint32_t *chunks, uint32_t n, const uint8_t *make_mesh, int lod_max,
+			  int nthreads, const int16_t *svl, uint64_t svl_len, const int16_t *vbo, uint64_t vbo_len,
+			  const uint32_t *ibo, uint64_t ibo_len, const uint64_t *svl_off, const uint32_t *svl_items,
+			  const uint64_t *vbo_off, const uint32_t *vbo_items, const uint64_t *ibo_off,
+			  const uint32_t *ibo_items, const uint32_t *status, uint32_t *bad, uint32_t bad_cap);
 
 #ifdef __cplusplus
 }
