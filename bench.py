@@ -32,6 +32,8 @@ CAMERA = (1024.0, 160.0, 1024.0)
 MESH_RADIUS = 512.0
 L2_FLUSH_BYTES = 512 << 20
 E2E_SLABS = 4
+SERVE_SLOTS = 4
+SERVE_MAX_BATCH = 64
 
 
 def peaks():
@@ -281,8 +283,10 @@ def run_ours(args):
     geo_avg_ms = geo_ms / args.steps
     peak, peak_kind = peaks()
     achieved = ab / (geo_avg_ms / 1e3) / 1e9
-    splat_bytes = int(res["svl_total"].astype(np.int64).sum()) * 2
-    step_bytes = ab + 2 * splat_bytes  # + grouping: splats read and written once more
+    # + grouping: the splats of levels >= 1 are read and written once more
+    # (a level-0 node is one chunk's level-0 segment, used where it lies)
+    grouped_bytes = int(res["svl_items"][:, 1:].astype(np.int64).sum()) * 2
+    step_bytes = ab + 2 * grouped_bytes
     # plain path: one launch per chunk and pass, same world and modes
     dw.rebuild(LOD_MAX, persistent=False, plain=True)
     dw.finish()
@@ -442,9 +446,10 @@ def run_ours(args):
             fs = full_scale(ctx)
             res5, dw5 = fs.pop("_res"), fs.pop("_dw")
             rle5 = dw5.rle_bytes()
-            # step bytes: RLE in, splats out plus the grouped copy (read and
-            # write again), mesh out, the shadow map once
-            ab5 = rle5 + int(res5["svl_total"].astype(np.int64).sum()) * 2 * 3 \
+            # step bytes: RLE in, splats out plus the grouped copy of levels
+            # >= 1 (read and written again), mesh out, the shadow map once
+            ab5 = rle5 + int(res5["svl_total"].astype(np.int64).sum()) * 2 \
+                + int(res5["svl_items"][:, 1:].astype(np.int64).sum()) * 2 * 2 \
                 + int(res5["vbo_items"].astype(np.int64).sum()) * 2 + int(res5["ibo_items"].astype(np.int64).sum()) * 4 \
                 + 16896 * 16384 * 2
             fs["rle_gb"] = round(rle5 / 1e9, 3)
@@ -564,8 +569,8 @@ def edit_serving(ctx, seconds=2.0, rate=2000.0, seed=4):
     rebuild_s = time.perf_counter() - t0
     edits = edit_trace(seed, int(seconds * rate), rate, 8192)
     warm = edit_trace(seed + 1, 200, rate, 8192)
-    dw.serve(warm, max_batch=64)
-    lat, st = dw.serve(edits, max_batch=64)
+    dw.serve(warm, max_batch=SERVE_MAX_BATCH, slots=SERVE_SLOTS)
+    lat, st = dw.serve(edits, max_batch=SERVE_MAX_BATCH, slots=SERVE_SLOTS)
     out = {
         "workload": "8192x512x8192 world (128x8x128 chunks of 64^3), small terrain, RLE-resident; "
                     "Poisson sphere edits at %d/s, r~U[1,32], 50%% carve / 50%% fill, centres in y 8..56" % rate,
@@ -577,6 +582,10 @@ def edit_serving(ctx, seconds=2.0, rate=2000.0, seed=4):
         "mean_batch": round(st.edits / max(st.batches, 1), 2),
         "max_batch": int(st.max_batch),
         "deferred": int(st.deferred),
+        "rejected": int(st.rejected),
+        "slots": SERVE_SLOTS,
+        "max_inflight": int(st.max_inflight),
+        "mean_inflight_when_busy": round(st.inflight_s / max(st.busy_s, 1e-9), 3),
         "chunks_remeshed_per_s": round(st.chunks_remeshed / st.wall_s, 1),
         "gpu_busy_frac": round(st.busy_s / st.wall_s, 3),
         "world_gen_s": round(gen_s, 2),
@@ -680,6 +689,28 @@ def full_scale(ctx, steps=3):
     torch.cuda.synchronize()
     ms = float(np.median([a_.elapsed_time(b_) for a_, b_ in evs]))
     shell_ms, geo_ms, grp_ms, _ = dw.kernel_ms()
+    handoff_gb = dw.handoff_bytes() / 1e9
+    # the same rebuilds with the decoded-chunk handoff off (the geometry
+    # pass decodes every chunk again): which of the two is faster here
+    dw.set_handoff(False)
+    dw.rebuild(5, group=True)
+    dw.finish()
+    dw.kernel_ms()
+    evs_off = []
+    for _ in range(steps):
+        a_ = torch.cuda.Event(enable_timing=True)
+        b_ = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a_.record(stream)
+        dw.rebuild(5, group=True)
+        with torch.cuda.stream(stream):
+            b_.record(stream)
+        evs_off.append((a_, b_))
+    ctx.sync()
+    torch.cuda.synchronize()
+    ms_off = float(np.median([a_.elapsed_time(b_) for a_, b_ in evs_off]))
+    shell_off, geo_off, grp_off, _ = dw.kernel_ms()
+    dw.set_handoff(True)
     ctx.set_timing(False)
     splats = int(res["svl_total"].astype(np.int64).sum()) // 4
     faces = int(res["ibo_items"].astype(np.int64).sum()) // 6
@@ -692,6 +723,10 @@ def full_scale(ctx, steps=3):
         "voxels_per_s": round(n * 64 ** 3 / (ms / 1e3), 1),
         "kernel_ms": {"shell": round(shell_ms / steps, 3), "geometry": round(geo_ms / steps, 3),
                       "group": round(grp_ms / steps, 3)},
+        "handoff_gb": round(handoff_gb, 3),
+        "handoff_off": {"ms_per_rebuild": round(ms_off, 3),
+                        "kernel_ms": {"shell": round(shell_off / steps, 3), "geometry": round(geo_off / steps, 3),
+                                      "group": round(grp_off / steps, 3)}},
         "splats": splats,
         "faces": faces,
         "mesh_chunks": int(modes.sum()),

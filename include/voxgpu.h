@@ -49,6 +49,7 @@ extern "C" {
 
 typedef struct vp_ctx vp_ctx;
 typedef struct vp_world vp_world;
+typedef struct vp_server vp_server;
 
 /* Result of one chunk; offsets index the world's output arenas. Item counts
  * are in the reference's units: int16 elements for splats and vertices
@@ -97,6 +98,17 @@ VP_API int vp_world_upload(vp_world *w, const uint32_t *pool, uint64_t pool_word
  * 8..56), kind 2 = terrain + caves (heights 40..200); horizontal noise
  * scaled by 2^hshift; the shadow map gets pad_rows zero rows. */
 VP_API int vp_world_generate(vp_world *w, int kind, uint64_t seed, int hshift, uint32_t pad_rows);
+
+/* The decoded-chunk handoff of full rebuilds: the shell pass decodes every
+ * chunk and, with the handoff on (the default), stores each multi-run
+ * chunk's decoded rows (20 * root^2 bytes) for the geometry pass to load
+ * instead of decoding again. The buffer is allocated at the first rebuild
+ * when the device keeps 4 GiB free beside it and it is at most a quarter of
+ * the device; otherwise, or with the handoff off, the geometry pass decodes.
+ * Outputs are the same either way. vp_world_handoff_bytes reports the
+ * buffer's size (0 when there is none). */
+VP_API int vp_world_set_handoff(vp_world *w, int on);
+VP_API int vp_world_handoff_bytes(vp_world *w, uint64_t *bytes);
 
 /* Per chunk: 1 = quad mesh (near chunk, ChunkMD.make_mesh), 0 = splats.
  * NULL = every chunk splats. */
@@ -171,10 +183,13 @@ typedef struct vp_serve_stats {
 	uint32_t batches;
 	uint32_t edits;
 	uint32_t max_batch;
-	uint32_t deferred;  /* times an edit waited for free HBM */
+	uint32_t deferred;  /* times the next batch waited: no free slot, or it touched in-flight work */
 	uint64_t chunks_remeshed;
-	double busy_s;      /* time with a batch on the GPU */
+	double busy_s;      /* time with at least one batch on the GPU */
 	double wall_s;
+	uint32_t max_inflight; /* most batches on the GPU at once */
+	uint32_t rejected;  /* edits refused: alone they need more than a slot holds */
+	double inflight_s;  /* integral of batches on the GPU over time (/ busy_s = mean overlap) */
 } vp_serve_stats;
 
 /* Apply edits[0..n) as one batch and rebuild the dirty chunks (synchronous). */
@@ -187,22 +202,74 @@ VP_API int vp_world_read_shadow(vp_world *w, uint16_t *dst, uint64_t n);
 VP_API int vp_world_rle_words(vp_world *w, uint64_t *words);
 /* The chunks the last edit batch rebuilt. */
 VP_API int vp_world_dirty(vp_world *w, uint32_t *chunks, uint32_t cap, uint32_t *n);
-/* Replay a timed edit trace (arrival_s ascending) in real time with
- * continuous batching: edits arriving while a batch runs queue up; the next
- * batch takes the queued edits in order, up to max_batch, as long as its
- * working memory fits the free HBM minus hbm_reserve bytes. latency_ms[i] =
- * completion of edit i's batch - its arrival. */
-VP_API int vp_world_serve(vp_world *w, const vp_edit *edits, uint32_t n, uint32_t max_batch, uint64_t hbm_reserve,
-			  double *latency_ms, vp_serve_stats *stats);
+/* Replay a timed edit trace (arrival_s ascending) in real time through an
+ * edit server (vp_server_create with `slots` slots of slot_chunks = 512,
+ * this max_batch and hbm_reserve): edits are submitted at their arrival
+ * times and batches overlap on the device as the server admits them.
+ * latency_ms[i] = the time edit i's batch was seen finished - its arrival
+ * (negative for an edit the server refused). */
+VP_API int vp_world_serve(vp_world *w, const vp_edit *edits, uint32_t n, uint32_t max_batch, uint32_t slots,
+			  uint64_t hbm_reserve, double *latency_ms, vp_serve_stats *stats);
+
+/* Edit server: continuous batching of world edits with requests in flight
+ * on the device at once (the reference's edit -> dirty -> next mesher tick
+ * flow, src/chunkset/edit.c:179-244, src/chunkset.c:246-309, as a request
+ * loop). Edits are applied in submission order. The server keeps up to
+ * `slots` batches on the GPU, each on its own stream with its own buffers
+ * for `slot_chunks` dirty chunks; a new batch is formed from the queue head
+ * (at most max_batch edits, at most slot_chunks dirty chunks) and admitted
+ * when a slot is free and it touches nothing an in-flight batch touches
+ * (chunks within one chunk of each other's dirty chunks, or sun-shadow map
+ * rows both use), so every batch's result is the one serial application
+ * gives. Slots are sized at creation from the device's free memory minus
+ * hbm_reserve: fewer slots when memory is short, VP_ENOMEM when not even
+ * one fits. An edit whose own dirty chunks exceed a slot completes with
+ * status VP_ENOMEM and changes nothing. Other calls on the world first wait
+ * for the server's in-flight batches. */
+typedef struct vp_server_config {
+	uint32_t slots;       /* batches on the GPU at once, 1..8 */
+	uint32_t max_batch;   /* edits per batch */
+	uint32_t slot_chunks; /* dirty chunks one batch may hold */
+	uint64_t hbm_reserve; /* device bytes the slots must leave free */
+} vp_server_config;
+
+/* One finished edit: its ticket, status (VP_OK, or VP_ENOMEM when refused),
+ * the batch it ran in, and host times in seconds since the server started:
+ * submitted, its batch admitted to the GPU, its batch seen finished. */
+typedef struct vp_edit_done {
+	uint64_t ticket;
+	int32_t status;
+	uint32_t batch;
+	double submit_s, start_s, done_s;
+} vp_edit_done;
+
+VP_API int vp_server_create(vp_world *w, const vp_server_config *cfg, vp_server **out);
+/* Waits for the in-flight batches, then frees the server. */
+VP_API void vp_server_destroy(vp_server *s);
+/* Queue edits; they get consecutive tickets from *first_ticket. Does not
+ * wait for the GPU: it retires finished batches and admits new ones. */
+VP_API int vp_edit_submit(vp_server *s, const vp_edit *edits, uint32_t n, uint64_t *first_ticket);
+/* Retire finished batches, admit queued edits, and return up to cap
+ * finished edits (*n of them, in completion order). With wait_us > 0 it
+ * keeps pumping for up to wait_us microseconds until at least one edit has
+ * finished. */
+VP_API int vp_poll_results(vp_server *s, vp_edit_done *out, uint32_t cap, uint32_t *n, uint32_t wait_us);
+/* Run every queued and in-flight edit to completion. */
+VP_API int vp_server_drain(vp_server *s);
+VP_API int vp_server_stats(vp_server *s, vp_serve_stats *stats, uint32_t *slots_out);
 
 /* LOD/octree draw groups of the last rebuild made with VP_REBUILD_GROUP
  * (gfx_update_svl, src/gfx/vsplat.c:209-331, minus the GL upload): for LOD
  * `lod`, node i (numbered flatten3(node, max_bitw - min(lod, max_bitw)))
  * holds the concatenated level-`lod` splats of its member chunks, scanned x
- * outer, y, z inner; off[i] / items[i] locate it in the group arena, in
- * int16 units. n = number of nodes to read (at most the chunk count). */
+ * outer, y, z inner; off[i] / items[i] locate it, in int16 units. At LOD 0
+ * every node is one chunk and its list is that chunk's level-0 segment, so
+ * the LOD-0 offsets index the splat arena (nothing is copied); the lists of
+ * LOD >= 1 nodes are concatenated in the group arena. n = number of nodes
+ * to read (at most the chunk count). vp_world_read_group reads n items of
+ * a LOD-`lod` node list at `off`. */
 VP_API int vp_world_group_nodes(vp_world *w, int lod, uint64_t *off, uint32_t *items, uint32_t n);
-VP_API int vp_world_read_group(vp_world *w, uint64_t off, uint64_t n, int16_t *dst);
+VP_API int vp_world_read_group(vp_world *w, int lod, uint64_t off, uint64_t n, int16_t *dst);
 
 /* RLE codec on host buffers (the device does the work). vp_rle_encode is
  * rle_compress (src/chunkset/rle.c:44-87): out receives the stream

@@ -29,14 +29,14 @@
 extern "C" {
 #endif
 
-/* src/chunkset/mesher.h:17-24 */
+/* src/chunkset/mesher.h:7-14 */
 VP_API void chunk_make_mesh(struct ChunkSet *setp, struct ChunkMD *cp, int16_t *geometry, uint32_t *geometry_items,
 			    uint32_t *index, uint32_t *index_items);
-/* src/chunkset/mesher.h:27-31 */
+/* src/chunkset/mesher.h:17-21 */
 VP_API void chunk_make_mask(struct ChunkSet *setp, struct ChunkMD *cp, uint8_t *mask);
-/* src/chunkset/mesher.h:33-38 */
+/* src/chunkset/mesher.h:23-28 */
 VP_API void chunk_mask_downsample(struct ChunkSet *setp, int8_t lod, Voxel *mask, Voxel *work);
-/* src/chunkset/mesher.h:40-47 */
+/* src/chunkset/mesher.h:30-37 */
 VP_API void chunk_make_splatlist(struct ChunkSet *setp, struct ChunkMD *cp, uint8_t level, Voxel *mask,
 				 int16_t *geometry, uint32_t *geometry_items);
 /* src/chunkset/rle.h:7-8; the returned buffer comes from the allocator set

@@ -31,10 +31,19 @@ def build_oracle(force=False):
     return LIBVPO
 
 
+def reference_root():
+    """Where the reference tree is looked for: VP_REFERENCE, else the
+    default of the build recipe (build_ref.sh, the one place that names it)."""
+    if os.environ.get("VP_REFERENCE"):
+        return os.environ["VP_REFERENCE"]
+    out = subprocess.run(["sh", os.path.join(HERE, "build_ref.sh"), "--root"], capture_output=True, text=True)
+    return out.stdout.strip()
+
+
 def build_ref(force=False):
     """Returns the path of libvpref.so, or None without the reference tree."""
     script = os.path.join(HERE, "build_ref.sh")
-    ref = os.environ.get("VP_REFERENCE", "/root/reference")
+    ref = reference_root()
     if not os.path.exists(os.path.join(ref, "src", "chunkset", "mesher.c")):
         return None
     srcs = [script, os.path.join(HERE, "ref_harness.c"),

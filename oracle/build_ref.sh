@@ -6,6 +6,12 @@
 set -e
 REF=${VP_REFERENCE:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+# `build_ref.sh --root` prints where the reference tree is looked for
+# (VP_REFERENCE, else the checkout this recipe was written against)
+if [ "$1" = "--root" ]; then
+	echo "$REF"
+	exit 0
+fi
 OUT="$HERE/_ref"
 if [ ! -f "$REF/src/chunkset/mesher.c" ]; then
 	echo "reference sources not found under $REF" >&2

@@ -4,7 +4,8 @@ Runs the unmodified reference hot-path sources, compiled by
 oracle/build_ref.sh into oracle/_ref/libvpref.so, on small seeded worlds
 and records inputs (RLE streams + shadow map) and outputs (splat lists per
 LOD, quad meshes, RLE encodings, sphere-edit results). Needs the reference
-tree (VP_REFERENCE, default /root/reference); run from the repository root:
+tree (VP_REFERENCE, else the default of oracle/build_ref.sh); run from the
+repository root:
 
     python tests/golden/make_golden.py
 """

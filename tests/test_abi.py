@@ -51,7 +51,8 @@ def _probe(tmp_path, name, extra):
 
 
 def test_chunkset_layout_matches_reference(tmp_path):
-    ref = os.environ.get("VP_REFERENCE", "/root/reference")
+    from oracle.build import reference_root
+    ref = reference_root()
     if not os.path.exists(os.path.join(ref, "src", "chunkset.h")):
         pytest.skip("reference sources not present")
     ours = _probe(tmp_path, "ours", ["-I", INCLUDE])

@@ -42,7 +42,7 @@ def test_group_matches_oracle(ctx, root_bitw, max_bitw, lod_max):
                 for nx in range(1 << ob[0]):
                     idx = ((nz << ob[1] | ny) << ob[0]) | nx
                     want = o.group_node(lod, (nx, ny, nz), svl, items)
-                    got = dw.read_group(off[idx], nit[idx])
+                    got = dw.read_group(lod, off[idx], nit[idx])
                     assert np.array_equal(got, want), (lod, nx, ny, nz)
 
 
@@ -87,7 +87,7 @@ def test_overflowing_arenas_grow_and_rerun(ctx):
         for lod in range(5):
             off, nit = dw.group_nodes(lod)
             nodes = 1 << sum(b - min(lod, b) for b in (2, 3, 2))
-            groups.append([dw.read_group(off[i], nit[i]) for i in range(nodes)])
+            groups.append([dw.read_group(lod, off[i], nit[i]) for i in range(nodes)])
         got.append((geo, groups))
         dw.close()
     (ga, gra), (gb, grb) = got

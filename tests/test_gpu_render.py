@@ -29,7 +29,7 @@ def oracle_frame(dw, cam, mq, sq, res):
         if lod not in offs:
             offs[lod] = dw.group_nodes(lod)
         off, items = offs[lod]
-        f.splats(dw.read_group(off[node], items[node]), lod)
+        f.splats(dw.read_group(lod, off[node], items[node]), lod)
     return f
 
 

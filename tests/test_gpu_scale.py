@@ -63,7 +63,7 @@ def _group_nodes_match(dw, res, svl, max_bitw, lod_max, modes):
                              idx >> (ob_[0] + ob_[1])], np.uint32)
             m = lib.vpo_group_node(o.h, lod, node.ctypes.data, ctypes.cast(ptrs, ctypes.c_void_p),
                                    ctypes.cast(iptrs, ctypes.c_void_p), want.ctypes.data)
-            got = dw.read_group(off[idx], nit[idx])
+            got = dw.read_group(lod, off[idx], nit[idx])
             if not np.array_equal(got, want[:m]):
                 bad.append((lod, idx))
     return bad

@@ -251,6 +251,7 @@ VP_API void vp_world_destroy(vp_world *w)
 	dev_free(w->d_big);
 	dev_free(w->d_check);
 	dev_free(w->d_dec);
+	dev_free(w->d_dec_slot);
 	dev_free(w->d_cull_slots);
 	dev_free(w->d_cull_blocks);
 	dev_free(w->d_cull_out);
@@ -287,18 +288,7 @@ VP_API void vp_world_destroy(vp_world *w)
 	dev_free(w->d_node_off);
 	dev_free(w->d_node_items);
 	dev_free(w->d_garena);
-	dev_free(w->d_vols);
-	dev_free(w->d_edit_chunks);
-	dev_free(w->d_dirty);
-	dev_free(w->d_edit_items);
-	dev_free(w->d_new_off);
-	dev_free(w->d_new_len);
-	dev_free(w->d_edit_sc);
-	dev_free(w->d_tile_scratch);
-	dev_free(w->d_nruns);
-	dev_free(w->d_run_scratch);
-	if (w->h_pin) cudaFreeHost(w->h_pin);
-	if (w->edit_done) cudaEventDestroy(w->edit_done);
+	vpi_edit_state_free(w);
 	for (cudaEvent_t e : w->ev) cudaEventDestroy(e);
 	delete w;
 }
@@ -524,6 +514,30 @@ VP_API int vp_world_generate(vp_world *w, int kind, uint64_t seed, int hshift, u
 	return vpi_upload_setdesc(w);
 }
 
+VP_API int vp_world_set_handoff(vp_world *w, int on)
+{
+	if (!w) return VP_EINVAL;
+	CK(cudaSetDevice(w->ctx->device));
+	int rc = vpi_pipe_drain(w);
+	if (rc) return rc;
+	CK(cudaStreamSynchronize(w->ctx->stream));
+	w->handoff = on != 0;
+	w->dec_failed = false;
+	if (!w->handoff) {
+		dev_free(w->d_dec);
+		dev_free(w->d_dec_slot);
+		w->dec_bytes = 0;
+	}
+	return VP_OK;
+}
+
+VP_API int vp_world_handoff_bytes(vp_world *w, uint64_t *bytes)
+{
+	if (!w || !bytes) return VP_EINVAL;
+	*bytes = w->d_dec ? w->dec_bytes : 0u;
+	return VP_OK;
+}
+
 VP_API int vp_world_set_modes(vp_world *w, const uint8_t *make_mesh)
 {
 	if (!w) return VP_EINVAL;
@@ -564,15 +578,32 @@ static int ensure_items(vp_world *w)
 
 uint8_t *vpi_decoded(vp_world *w)
 {
-	const size_t need = (size_t)w->nchunks * decoded_bytes_per_chunk(w->root_bitw);
-	if (!need || w->dec_failed) return nullptr;
-	if (w->d_dec && w->dec_bytes >= need) return w->d_dec;
+	const size_t per = decoded_bytes_per_chunk(w->root_bitw);
+	if (!per || !w->handoff || w->dec_failed) return nullptr;
+	if (w->d_dec) return w->d_dec;
+	/* one slot per chunk of more than one run (single-run chunks decode in
+	 * no time); chunks whose length changes later keep or lack a slot,
+	 * which only decides whether the geometry pass loads or decodes */
+	std::vector<uint32_t> slot(w->nchunks, kNoSlot);
+	uint32_t k = 0;
+	for (uint32_t c = 0; c < w->nchunks; c++)
+		if (c < w->hlen.size() && w->hlen[c] > 2u) slot[c] = k++;
+	const size_t need = (size_t)k * per;
 	size_t free_b = 0, total_b = 0;
-	/* keep 4 GiB free for arenas and the rest; without room, decode twice */
-	if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || free_b < need + (4ull << 30) ||
-	    cudaMalloc(&w->d_dec, need) != cudaSuccess) {
+	/* keep 4 GiB free for arenas and the rest, and at most a quarter of the
+	 * device; without room, decode twice */
+	if (!k || cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || free_b < need + (4ull << 30) ||
+	    need > total_b / 4 || cudaMalloc(&w->d_dec, need) != cudaSuccess) {
 		cudaGetLastError();
 		w->d_dec = nullptr;
+		w->dec_failed = true;
+		return nullptr;
+	}
+	if (dev_alloc(&w->d_dec_slot, w->nchunks) ||
+	    cudaMemcpy(w->d_dec_slot, slot.data(), w->nchunks * 4u, cudaMemcpyHostToDevice) != cudaSuccess) {
+		cudaGetLastError();
+		dev_free(w->d_dec);
+		dev_free(w->d_dec_slot);
 		w->dec_failed = true;
 		return nullptr;
 	}
@@ -672,6 +703,7 @@ static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 	L.outs = w->d_outs;
 	L.lod_max = lod_max;
 	L.decoded = vpi_decoded(w); /* every chunk is shelled before any geometry */
+	L.dec_slot = w->d_dec_slot;
 	Arena *ar[3] = {&L.svl, &L.vbo, &L.ibo};
 	for (int a = 0; a < 3; a++) {
 		ar[a]->base = w->d_arena[a];
@@ -1006,6 +1038,7 @@ VP_API int vp_world_render(vp_world *w, const vp_camera *cam, const uint32_t *me
 	a.light[1] = 1.0f / llen;
 	a.light[2] = 0.0f / llen;
 	a.splats = w->d_garena;
+	a.splats_l0 = (const int16_t *)w->d_arena[0];
 	a.segs = (const RenderSeg *)(R + o_seg);
 	a.seg_first = (const uint64_t *)(R + o_sf);
 	a.nseg = n_svl;
@@ -1063,6 +1096,7 @@ static int settle_half(vp_world *w, int h)
 int vpi_pipe_drain(vp_world *w)
 {
 	int rc;
+	if ((rc = vpi_server_quiesce(w))) return rc;
 	const int older = w->pipe_half; /* the next half to be used was written first */
 	if ((rc = settle_half(w, older)) || (rc = settle_half(w, older ^ 1))) return rc;
 	return VP_OK;
@@ -1146,6 +1180,7 @@ static int stream_rebuild(vp_world *w, int lod_max, unsigned flags, int slabs, v
 	L.outs = w->d_outs;
 	L.lod_max = lod_max;
 	L.decoded = vpi_decoded(w); /* every chunk is shelled before the slabs */
+	L.dec_slot = w->d_dec_slot;
 	Arena *ar[3] = {&L.svl, &L.vbo, &L.ibo};
 	for (int a = 0; a < 3; a++) {
 		ar[a]->base = w->d_arena[a];
@@ -1320,10 +1355,11 @@ VP_API int vp_world_group_nodes(vp_world *w, int lod, uint64_t *off, uint32_t *i
 	return VP_OK;
 }
 
-VP_API int vp_world_read_group(vp_world *w, uint64_t off, uint64_t n, int16_t *dst)
+VP_API int vp_world_read_group(vp_world *w, int lod, uint64_t off, uint64_t n, int16_t *dst)
 {
-	if (!w || (!dst && n) || !w->d_garena) return VP_EINVAL;
-	if ((off + n) * 2u > w->garena_units * 16u) return VP_EINVAL;
+	if (!w || (!dst && n) || lod < 0 || lod > w->grouped_lod) return VP_EINVAL;
+	if (lod == 0) return vp_world_read_svl(w, off, n, dst);
+	if (!w->d_garena || (off + n) * 2u > w->garena_units * 16u) return VP_EINVAL;
 	if (!n) return VP_OK;
 	CK(cudaMemcpyAsync(dst, w->d_garena + off, n * 2u, cudaMemcpyDeviceToHost, w->ctx->stream));
 	CK(cudaStreamSynchronize(w->ctx->stream));

@@ -63,6 +63,9 @@ struct ChunkOut {
 
 enum : uint32_t { kStatusOverflow = 1u, kStatusBadStream = 2u };
 
+/* no slot (handoff table of decoded chunks) */
+constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
+
 /* A bump-allocated output arena, allocation unit 16 bytes. */
 struct Arena {
 	void *base;

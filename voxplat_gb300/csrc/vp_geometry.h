@@ -19,11 +19,14 @@ struct GeoLaunch {
 	int lod_max;
 	uint8_t *big_scratch;       /* 128^3 chunks: per-CTA working sets */
 	uint32_t big_slots;         /* slots in big_scratch = CTAs of a launch */
-	/* <= 64^3 chunks, or NULL: decoded_bytes_per_chunk() per chunk. The
-	 * shell pass stores each chunk it decodes there; the geometry pass
-	 * loads them instead of decoding, so a launch pair that passes it must
-	 * shell every non-empty chunk whose geometry it builds. */
+	/* <= 64^3 chunks, or NULL: decoded chunks handed from the shell pass
+	 * to the geometry pass, decoded_bytes_per_chunk() each, chunk c in slot
+	 * dec_slot[c] (kNoSlot: not handed over, the geometry pass decodes it).
+	 * The shell pass stores each chunk it decodes that has a slot; the
+	 * geometry pass loads those instead of decoding, so a launch pair that
+	 * passes it must shell every non-empty chunk whose geometry it builds. */
 	uint8_t *decoded;
+	const uint32_t *dec_slot;
 };
 
 size_t geometry_smem_bytes(int root_bitw);

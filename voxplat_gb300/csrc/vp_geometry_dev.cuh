@@ -334,7 +334,7 @@ __device__ void load_decoded(const uint8_t *src, const Smem &m)
 
 template <int RB>
 __global__ void __launch_bounds__(512, 2) k_shell(const SetDesc *__restrict__ sets, const WorkItem *__restrict__ items,
-					       uint32_t nitems, uint8_t *decoded)
+					       uint32_t nitems, uint8_t *decoded, const uint32_t *__restrict__ dec_slot)
 {
 	using G = Geo<RB>;
 	constexpr int R = G::R, RR = G::RR;
@@ -348,7 +348,10 @@ __global__ void __launch_bounds__(512, 2) k_shell(const SetDesc *__restrict__ se
 	if (chunk_is_null(S, wi.chunk, N)) return;
 	const uint32_t *stream = S.pool + S.off[wi.chunk];
 	decode_chunk<RB>(stream, S.len[wi.chunk] - 1u, m);
-	if (decoded) store_decoded<RB>(m, decoded + (size_t)wi.chunk * G::dec_bytes);
+	if (decoded) {
+		const uint32_t ds = dec_slot[wi.chunk];
+		if (ds != kNoSlot) store_decoded<RB>(m, decoded + (size_t)ds * G::dec_bytes);
+	}
 	uint64_t *bits = S.shell_bits + (size_t)wi.chunk * G::shell_words;
 	uint8_t *cols = S.shell_col + (size_t)wi.chunk * G::shell_cols;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -1254,7 +1257,7 @@ __device__ void mask_dense(const SetDesc &S, const uint32_t *__restrict__ stream
 template <int RB>
 __device__ __forceinline__ void geometry_item(const SetDesc &S, const WorkItem &wi, ChunkOut *out, const Smem &m,
 					      const Arena &asvl, const Arena &avbo, const Arena &aibo, int lod_max,
-					      const uint8_t *decoded = nullptr)
+					      const uint8_t *decoded = nullptr, const uint32_t *dec_slot = nullptr)
 {
 	using G = Geo<RB>;
 	constexpr int R = G::R;
@@ -1279,8 +1282,9 @@ __device__ __forceinline__ void geometry_item(const SetDesc &S, const WorkItem &
 	}
 	const uint32_t *stream = S.pool + S.off[wi.chunk];
 	/* the shell pass of this rebuild stored every chunk but the all-air ones */
-	if (decoded && !chunk_is_null(S, wi.chunk, N))
-		load_decoded<RB>(decoded + (size_t)wi.chunk * G::dec_bytes, m);
+	const uint32_t ds = decoded && !chunk_is_null(S, wi.chunk, N) ? dec_slot[wi.chunk] : kNoSlot;
+	if (ds != kNoSlot)
+		load_decoded<RB>(decoded + (size_t)ds * G::dec_bytes, m);
 	else
 		decode_chunk<RB>(stream, S.len[wi.chunk] - 1u, m);
 	load_halo<RB>(S, m);
@@ -1296,7 +1300,8 @@ __device__ __forceinline__ void geometry_item(const SetDesc &S, const WorkItem &
 template <int RB>
 __global__ void __launch_bounds__(512, 2) k_geometry(const SetDesc *__restrict__ sets, const WorkItem *__restrict__ items,
 						     uint32_t nitems, unsigned int *queue, ChunkOut *outs, Arena asvl,
-						     Arena avbo, Arena aibo, int lod_max, const uint8_t *decoded)
+						     Arena avbo, Arena aibo, int lod_max, const uint8_t *decoded,
+						     const uint32_t *__restrict__ dec_slot)
 {
 	extern __shared__ __align__(16) uint8_t smem[];
 	const Smem m = carve<RB>(smem);
@@ -1310,7 +1315,7 @@ __global__ void __launch_bounds__(512, 2) k_geometry(const SetDesc *__restrict__
 		next = nitems;
 		const WorkItem wi = items[it];
 		const SetDesc S = sets[wi.set];
-		geometry_item<RB>(S, wi, outs + wi.slot, m, asvl, avbo, aibo, lod_max, decoded);
+		geometry_item<RB>(S, wi, outs + wi.slot, m, asvl, avbo, aibo, lod_max, decoded, dec_slot);
 	}
 }
 
@@ -1368,14 +1373,15 @@ static cudaError_t launch_rb(const GeoLaunch &L, cudaStream_t st)
 	e = cudaFuncSetAttribute(k_geometry<RB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::bytes);
 	if (e != cudaSuccess) return e;
 	if (L.run_shell && L.n_shell) {
-		k_shell<RB><<<L.n_shell, L.threads, G::bytes, st>>>(L.sets, L.shell_items, L.n_shell, L.decoded);
+		k_shell<RB><<<L.n_shell, L.threads, G::bytes, st>>>(L.sets, L.shell_items, L.n_shell, L.decoded,
+								     L.dec_slot);
 		e = cudaGetLastError();
 		if (e != cudaSuccess) return e;
 	}
 	if (L.n_items) {
 		const uint32_t grid = L.queue ? L.ctas : L.n_items;
 		k_geometry<RB><<<grid, L.threads, G::bytes, st>>>(L.sets, L.items, L.n_items, L.queue, L.outs, L.svl, L.vbo,
-								 L.ibo, L.lod_max, L.decoded);
+								 L.ibo, L.lod_max, L.decoded, L.dec_slot);
 		e = cudaGetLastError();
 	}
 	return e;

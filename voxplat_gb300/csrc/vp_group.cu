@@ -8,13 +8,18 @@
  * splat segments in that order. Nodes are numbered flatten3(node,
  * max_bitw - min(l, max_bitw)) as in the reference.
  *
- * With power-of-two chunk counts every node is full, so
+ * At LOD 0 every node is one chunk, so a node's buffer is that chunk's
+ * level-0 segment as the geometry pass wrote it: the node table points into
+ * the splat arena and nothing is copied (level 0 holds most of the splats).
+ *
+ * For LOD >= 1, with power-of-two chunk counts every node is full, so
  *   key(c) = node_index(c) * members + member_rank(c)
  * is a bijection onto [0, nchunks): the prefix sum of the level-l item
  * counts in key order gives every segment's destination, and node i's
  * buffer starts at the prefix of its first key. One pass scatters counts
  * into key order, one CTA per level scans them, and a CTA per chunk copies
- * its segment with 8-byte vector moves (one splat per thread per step).
+ * its segment with 8-byte vector moves (one splat per thread per step) into
+ * the group arena, levels 1, 2, ... one after the other.
  *
  * A rebuild whose splat arena overflowed left some chunks without lists
  * (their records carry the overflow status); the copy is then skipped as a
@@ -108,20 +113,30 @@ __global__ void __launch_bounds__(1024) k_group_scan(uint32_t n, GroupArgs a)
 	if (threadIdx.x == 0) a.level_total[blockIdx.x] = s_carry;
 }
 
-/* one CTA per (chunk, level): copy the chunk's level-l segment, one splat
- * (8 bytes) per thread per step; the first member of each node also records
- * the node's offset and length */
+/* level 0: node c is chunk c, its list the chunk's level-0 segment in the
+ * splat arena */
+__global__ void k_group_level0(const ChunkOut *__restrict__ outs, uint32_t nchunks, GroupArgs a)
+{
+	const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+	if (c >= nchunks) return;
+	a.node_off[c] = outs[c].svl_off;
+	a.node_items[c] = outs[c].svl_items[0];
+}
+
+/* one CTA per (chunk, level >= 1): copy the chunk's level-l segment, one
+ * splat (8 bytes) per thread per step; the first member of each node also
+ * records the node's offset and length */
 __global__ void __launch_bounds__(256) k_group_copy(const ChunkOut *__restrict__ outs, uint32_t nchunks, GroupArgs a)
 {
 	const uint32_t c = blockIdx.x;
-	const int l = blockIdx.y;
+	const int l = blockIdx.y + 1;
 	if (c >= nchunks) return;
 	if (*a.svl_cursor > a.svl_cap_units) return; /* overflowed rebuild: rerun follows */
 	const GroupGeom g = group_geom(a.max_bitw, l);
 	uint32_t node, rank;
 	const uint32_t key = group_key(g, c, &node, &rank);
 	uint64_t lbase = 0;
-	for (int k = 0; k < l; k++) lbase += a.level_total[k];
+	for (int k = 1; k < l; k++) lbase += a.level_total[k];
 	const uint64_t *cnt = a.counts + (size_t)l * nchunks;
 	const uint64_t dst_off = lbase + cnt[key];
 	if (rank == 0 && threadIdx.x == 0) {
@@ -145,9 +160,12 @@ cudaError_t launch_group(const ChunkOut *outs, uint32_t nchunks, int lod_max, co
 {
 	if (!nchunks) return cudaSuccess;
 	const int L = lod_max + 1;
-	k_group_scatter<<<dim3((nchunks + 255) / 256, L), 256, 0, st>>>(outs, nchunks, a);
-	k_group_scan<<<L, 1024, 0, st>>>(nchunks, a);
-	k_group_copy<<<dim3(nchunks, L), 256, 0, st>>>(outs, nchunks, a);
+	k_group_level0<<<(nchunks + 255) / 256, 256, 0, st>>>(outs, nchunks, a);
+	if (L > 1) {
+		k_group_scatter<<<dim3((nchunks + 255) / 256, L), 256, 0, st>>>(outs, nchunks, a);
+		k_group_scan<<<L, 1024, 0, st>>>(nchunks, a);
+		k_group_copy<<<dim3(nchunks, L - 1), 256, 0, st>>>(outs, nchunks, a);
+	}
 	return cudaGetLastError();
 }
 

@@ -8,10 +8,11 @@ struct GroupArgs {
 	uint32_t max_bitw[3];
 	uint64_t *counts;      /* [levels][nchunks] scratch: counts, then prefixes */
 	uint64_t *level_total; /* [levels] int16 items per level */
-	uint64_t *node_off;    /* [levels][nchunks] node start in `out` (int16 units) */
+	uint64_t *node_off;    /* [levels][nchunks] node start (int16 units): level 0 in the
+	                        * splat arena, levels >= 1 in `out` */
 	uint32_t *node_items;  /* [levels][nchunks] node length (int16 units) */
 	const int16_t *svl;    /* per-chunk splat lists (the splat arena) */
-	int16_t *out;          /* grouped lists: level 0 nodes, then level 1 ... */
+	int16_t *out;          /* grouped lists of levels >= 1: level 1 nodes, then level 2 ... */
 	const unsigned long long *svl_cursor; /* the splat arena's bump cursor (16 B units) */
 	uint64_t svl_cap_units;               /* the splat arena's capacity (16 B units) */
 	uint64_t out_cap;                     /* capacity of `out` (int16 units) */

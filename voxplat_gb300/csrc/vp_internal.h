@@ -50,6 +50,8 @@ struct vp_ctx {
 
 constexpr int kMaxStreamSlabs = 16;
 
+struct EditSlot; /* one edit batch's device buffers, stream and bookkeeping (vp_serve.cu) */
+
 struct vp_world {
 	vp_ctx *ctx;
 	int root_bitw;
@@ -63,8 +65,10 @@ struct vp_world {
 	uint64_t shadow_len = 0;
 	uint64_t shadow_cap = 0;                 /* elements allocated in d_shadow */
 	uint8_t *d_dec = nullptr;                /* decoded chunks, shell pass -> geometry pass */
+	uint32_t *d_dec_slot = nullptr;          /* per chunk: its slot in d_dec, or kNoSlot */
 	size_t dec_bytes = 0;
 	bool dec_failed = false;                 /* no room: rebuilds decode twice */
+	bool handoff = true;                     /* vp_world_set_handoff */
 	uint32_t *d_check = nullptr;             /* upload validation: status, first bad chunk */
 	uint32_t *h_check = nullptr;             /* its mapped pinned copy, and that copy's device address */
 	uint32_t *h_check_dev = nullptr;
@@ -133,26 +137,11 @@ struct vp_world {
 	/* edits: the pool grows at its tail, re-encoded streams are appended */
 	uint64_t pool_cap = 0;                   /* words allocated in d_pool */
 	uint64_t pool_tail = 0;                  /* first free word */
-	uint8_t *d_vols = nullptr;               /* decoded volumes of an edit batch */
-	size_t vols_cap = 0;                     /* chunks */
-	void *d_edit_chunks = nullptr;           /* EditChunk lists of a batch */
-	size_t edit_chunks_cap = 0;
-	uint32_t *d_dirty = nullptr;             /* dirty chunk ids of a batch */
-	WorkItem *d_edit_items = nullptr;
-	uint64_t *d_new_off = nullptr;
-	uint32_t *d_new_len = nullptr;
-	size_t dirty_cap = 0;
-	unsigned long long *d_edit_sc = nullptr; /* [0] encode cursor, [1] status */
-	uint32_t *d_tile_scratch = nullptr;      /* tile sums of the tile-parallel codec */
-	size_t tile_cap = 0;
-	uint32_t *d_nruns = nullptr;
-	size_t nruns_cap = 0;
-	uint32_t *d_run_scratch = nullptr;       /* packed run starts while re-encoding */
-	size_t run_scratch_cap = 0;
-	unsigned long long *h_pin = nullptr;     /* pinned: encode cursor, status, 3 arena cursors */
-	std::vector<int32_t> slot_of;            /* chunk -> volume slot during a batch */
+	unsigned long long *d_pool_cursor = nullptr; /* device copy of the pool tail while edit batches append */
+	EditSlot *eslot = nullptr;               /* the synchronous edit path's batch state (vp_world_edit) */
+	vp_server *server = nullptr;             /* the edit server attached to this world, if any */
+	std::vector<int32_t> slot_of;            /* chunk -> volume slot while a batch is planned */
 	std::vector<uint32_t> last_dirty;
-	cudaEvent_t edit_done = nullptr;
 	uint64_t shadow_base = 0;                /* world index of d_shadow[0] */
 	std::vector<cudaEvent_t> ev;             /* pairs per kernel */
 	std::vector<int> ev_kind;                /* 0 shell, 1 geometry */
@@ -178,8 +167,13 @@ int vpi_world_shadow_window(vp_world *w, const uint16_t *map, uint64_t map_len, 
 int vpi_world_run(vp_world *w, const WorkItem *items, uint32_t n, int lod_max);
 /* A reference-format stream of n words (terminator included) covering N
  * voxels with nonzero run lengths. */
-/* waits for the copies of pipelined streamed rebuilds and rebases their results */
+/* waits for the copies of pipelined streamed rebuilds and rebases their
+ * results, and for the edit batches an attached server has in flight */
 extern "C" int vpi_pipe_drain(vp_world *w);
+/* vp_serve.cu: retire every in-flight batch of the world's server (no-op
+ * without one) and free the edit path's state at world destruction */
+int vpi_server_quiesce(vp_world *w);
+void vpi_edit_state_free(vp_world *w);
 /* the decoded-chunk handoff buffer of a full rebuild, or NULL (128^3 roots,
  * or not enough free device memory: the geometry pass then decodes) */
 extern "C" uint8_t *vpi_decoded(vp_world *w);

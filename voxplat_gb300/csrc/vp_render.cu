@@ -166,7 +166,7 @@ __device__ __forceinline__ const int16_t *splat_of(const RenderArgs &a, uint64_t
 	}
 	const RenderSeg sg = a.segs[lo];
 	lod = __int2float_rn(1 << sg.lod);
-	return a.splats + sg.off + (k - a.seg_first[lo]) * 4u;
+	return (sg.lod ? a.splats : a.splats_l0) + sg.off + (k - a.seg_first[lo]) * 4u;
 }
 
 __global__ void __launch_bounds__(256) k_draw_splats(RenderArgs a)

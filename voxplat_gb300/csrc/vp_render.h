@@ -28,7 +28,8 @@ struct RenderMesh {
 struct RenderArgs {
 	RenderCam cam;
 	float light[3];                 /* normalize(-1, 1, 0) */
-	const int16_t *splats;
+	const int16_t *splats;     /* grouped lists of LOD >= 1 nodes */
+	const int16_t *splats_l0;  /* the splat arena: LOD 0 nodes are chunks' level-0 segments */
 	const RenderSeg *segs;
 	const uint64_t *seg_first;      /* first splat of each segment */
 	uint32_t nseg;

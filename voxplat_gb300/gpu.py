@@ -77,7 +77,17 @@ class Camera(ctypes.Structure):
 class ServeStats(ctypes.Structure):
     _fields_ = [("batches", ctypes.c_uint32), ("edits", ctypes.c_uint32), ("max_batch", ctypes.c_uint32),
                 ("deferred", ctypes.c_uint32), ("chunks_remeshed", ctypes.c_uint64), ("busy_s", ctypes.c_double),
-                ("wall_s", ctypes.c_double)]
+                ("wall_s", ctypes.c_double), ("max_inflight", ctypes.c_uint32), ("rejected", ctypes.c_uint32),
+                ("inflight_s", ctypes.c_double)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("slots", ctypes.c_uint32), ("max_batch", ctypes.c_uint32), ("slot_chunks", ctypes.c_uint32),
+                ("hbm_reserve", ctypes.c_uint64)]
+
+
+EDIT_DONE_DTYPE = np.dtype([("ticket", np.uint64), ("status", np.int32), ("batch", np.uint32),
+                            ("submit_s", np.float64), ("start_s", np.float64), ("done_s", np.float64)])
 
 
 def make_edits(rows, arrival=None):
@@ -126,6 +136,8 @@ def load(build_if_missing=True):
         "vp_world_destroy": (None, [V]),
         "vp_world_upload": (I, [V, V, U64, V, V, V, U64, U32]),
         "vp_world_set_modes": (I, [V, V]),
+        "vp_world_set_handoff": (I, [V, I]),
+        "vp_world_handoff_bytes": (I, [V, ctypes.POINTER(U64)]),
         "vp_world_rebuild": (I, [V, I, ctypes.c_uint]),
         "vp_world_finish": (I, [V]),
         "vp_world_reserve": (I, [V, V]),
@@ -144,11 +156,17 @@ def load(build_if_missing=True):
         "vp_world_read_vbo": (I, [V, U64, U64, V]),
         "vp_world_read_ibo": (I, [V, U64, U64, V]),
         "vp_world_group_nodes": (I, [V, I, V, V, U32]),
-        "vp_world_read_group": (I, [V, U64, U64, V]),
+        "vp_world_read_group": (I, [V, I, U64, U64, V]),
         "vp_world_generate": (I, [V, I, U64, I, U32]),
         "vp_world_edit": (I, [V, V, U32]),
         "vp_world_dirty": (I, [V, V, U32, ctypes.POINTER(U32)]),
-        "vp_world_serve": (I, [V, V, U32, U32, U64, V, V]),
+        "vp_world_serve": (I, [V, V, U32, U32, U32, U64, V, V]),
+        "vp_server_create": (I, [V, V, PV]),
+        "vp_server_destroy": (None, [V]),
+        "vp_edit_submit": (I, [V, V, U32, ctypes.POINTER(U64)]),
+        "vp_poll_results": (I, [V, V, U32, ctypes.POINTER(U32), U32]),
+        "vp_server_drain": (I, [V]),
+        "vp_server_stats": (I, [V, V, ctypes.POINTER(U32)]),
         "vp_world_chunk_rle": (I, [V, U32, V, U32, ctypes.POINTER(U32)]),
         "vp_world_read_shadow": (I, [V, V, U64]),
         "vp_world_rle_words": (I, [V, ctypes.POINTER(U64)]),
@@ -295,6 +313,15 @@ class DeviceWorld:
         except Exception:
             pass
 
+    def set_handoff(self, on):
+        """Decoded-chunk handoff between the passes of a full rebuild."""
+        check(self.lib.vp_world_set_handoff(self.h, 1 if on else 0), "vp_world_set_handoff")
+
+    def handoff_bytes(self):
+        n = ctypes.c_uint64()
+        check(self.lib.vp_world_handoff_bytes(self.h, ctypes.byref(n)), "vp_world_handoff_bytes")
+        return n.value
+
     def set_modes(self, make_mesh):
         if make_mesh is None:
             check(self.lib.vp_world_set_modes(self.h, None), "vp_world_set_modes")
@@ -315,9 +342,10 @@ class DeviceWorld:
         check(self.lib.vp_world_group_nodes(self.h, lod, _p(off), _p(items), self.nchunks), "vp_world_group_nodes")
         return off, items
 
-    def read_group(self, off, n):
+    def read_group(self, lod, off, n):
+        """n int16 items of a LOD-`lod` node list at `off` (group_nodes)."""
         out = np.zeros(int(n), np.int16)
-        check(self.lib.vp_world_read_group(self.h, int(off), int(n), _p(out)), "vp_world_read_group")
+        check(self.lib.vp_world_read_group(self.h, int(lod), int(off), int(n), _p(out)), "vp_world_read_group")
         return out
 
     def reserve(self, svl_bytes, vbo_bytes, ibo_bytes):
@@ -448,12 +476,13 @@ class DeviceWorld:
         check(self.lib.vp_world_dirty(self.h, _p(out), len(out), ctypes.byref(n)), "vp_world_dirty")
         return out
 
-    def serve(self, edits, max_batch=64, hbm_reserve=1 << 30):
-        """Replay a timed trace; returns (latency_ms array, ServeStats)."""
+    def serve(self, edits, max_batch=64, hbm_reserve=1 << 30, slots=4):
+        """Replay a timed trace through an edit server with `slots` batches
+        in flight at most; returns (latency_ms array, ServeStats)."""
         edits = np.ascontiguousarray(edits, dtype=EDIT_DTYPE)
         lat = np.zeros(len(edits), np.float64)
         st = ServeStats()
-        check(self.lib.vp_world_serve(self.h, _p(edits), len(edits), max_batch, hbm_reserve, _p(lat),
+        check(self.lib.vp_world_serve(self.h, _p(edits), len(edits), max_batch, slots, hbm_reserve, _p(lat),
                                       ctypes.byref(st)), "vp_world_serve")
         return lat, st
 
@@ -481,6 +510,53 @@ class DeviceWorld:
     def chunk_mesh(self, res, c):
         r = res[c]
         return self.read_vbo(r["vbo_off"], r["vbo_items"]), self.read_ibo(r["ibo_off"], r["ibo_items"])
+
+
+class EditServer:
+    """Continuous batching of edits on a device world (vp_server_*): submit
+    edits as they arrive, poll for the finished ones."""
+
+    def __init__(self, world, slots=4, max_batch=16, slot_chunks=512, hbm_reserve=1 << 30):
+        self.world = world
+        self.lib = world.lib
+        cfg = ServerConfig(slots, max_batch, slot_chunks, hbm_reserve)
+        h = ctypes.c_void_p()
+        check(self.lib.vp_server_create(world.h, ctypes.byref(cfg), ctypes.byref(h)), "vp_server_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.vp_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, edits):
+        """Queue edits (EDIT_DTYPE rows); returns the first ticket."""
+        edits = np.ascontiguousarray(edits, dtype=EDIT_DTYPE)
+        t = ctypes.c_uint64()
+        check(self.lib.vp_edit_submit(self.h, _p(edits), len(edits), ctypes.byref(t)), "vp_edit_submit")
+        return t.value
+
+    def poll(self, cap=1024, wait_us=0):
+        """Finished edits (EDIT_DONE_DTYPE array, completion order)."""
+        out = np.zeros(cap, EDIT_DONE_DTYPE)
+        n = ctypes.c_uint32()
+        check(self.lib.vp_poll_results(self.h, _p(out), cap, ctypes.byref(n), wait_us), "vp_poll_results")
+        return out[:n.value].copy()
+
+    def drain(self):
+        check(self.lib.vp_server_drain(self.h), "vp_server_drain")
+
+    def stats(self):
+        st = ServeStats()
+        n = ctypes.c_uint32()
+        check(self.lib.vp_server_stats(self.h, ctypes.byref(st), ctypes.byref(n)), "vp_server_stats")
+        return st, n.value
 
 
 class DeviceBatch:
