@@ -386,11 +386,13 @@ typedef struct vp_batch vp_batch;
 #define VP_BATCH_SPLIT 1 /* one persistent launch per root size, run concurrently */
 
 typedef struct vp_batch_tune {
-	int strategy;   /* VP_BATCH_MIXED or VP_BATCH_SPLIT */
-	int min_blocks; /* MIXED: 2 = registers capped for two CTAs per SM, 1 = uncapped */
-	int order;      /* 0 = longest stream first, 1 = by root size then longest (SPLIT needs 1) */
-	uint32_t ctas;  /* MIXED: persistent CTAs, 0 = as many as fit */
-	float ms;       /* vp_batch_autotune: measured rebuild time of this configuration */
+	int strategy;     /* VP_BATCH_MIXED or VP_BATCH_SPLIT */
+	int min_blocks;   /* MIXED: 2 = registers capped for two CTAs per SM, 1 = uncapped */
+	int order;        /* 0 = longest stream first, 1 = by root size then longest (SPLIT needs 1) */
+	uint32_t ctas;    /* MIXED: persistent CTAs, 0 = as many as fit */
+	float ms;         /* vp_batch_autotune: measured rebuild time of this configuration */
+	uint32_t threads; /* threads per chunk (CTA) for chunks up to 64^3: 256 or 512 (0 = 512) */
+	uint32_t grain;   /* MIXED and the 128^3 launch: chunks per dequeue from the work queue (0 = 1) */
 } vp_batch_tune;
 
 VP_API int vp_batch_create(vp_ctx *ctx, uint32_t n, const int *root_bitw, vp_batch **out);
@@ -407,8 +409,12 @@ VP_API int vp_batch_set_modes(vp_batch *b, const uint8_t *make_mesh);
  * arena growth); otherwise the tuned configuration launched directly. */
 VP_API int vp_batch_rebuild(vp_batch *b, int lod_max, unsigned flags);
 VP_API int vp_batch_finish(vp_batch *b);
-/* Time every candidate configuration on this batch (graph replays), keep
- * the fastest; `tried` (capacity *ntried) receives each with its time. */
+/* Time candidate configurations on this batch (graph replays) and keep the
+ * fastest: first the strategies and orders, then, around the best of
+ * those, threads per chunk (256, 512), chunks per dequeue (1, 2, 4) and,
+ * for MIXED, the persistent grid (as many CTAs as fit, or one per SM).
+ * `tried` (capacity *ntried) receives each with its time; *ntried gets the
+ * number timed. */
 VP_API int vp_batch_autotune(vp_batch *b, int lod_max, vp_batch_tune *best, vp_batch_tune *tried, int *ntried);
 VP_API int vp_batch_set_tune(vp_batch *b, const vp_batch_tune *t);
 VP_API int vp_batch_get_tune(vp_batch *b, vp_batch_tune *t);

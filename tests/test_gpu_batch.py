@@ -51,13 +51,16 @@ def check_batch(b, modes, want):
             assert np.array_equal(g, want[k][0]), k
 
 
-@pytest.mark.parametrize("cfg", [("mixed", 2, 0), ("mixed", 1, 0), ("mixed", 2, 1), ("split", 2, 1)])
+# (strategy, min_blocks, order, threads per chunk, chunks per dequeue, CTAs)
+@pytest.mark.parametrize("cfg", [("mixed", 2, 0, 512, 1, 0), ("mixed", 1, 0, 512, 1, 0), ("mixed", 2, 1, 512, 1, 0),
+                                 ("split", 2, 1, 512, 1, 0), ("mixed", 2, 0, 256, 4, 0), ("mixed", 2, 0, 512, 2, 152),
+                                 ("split", 2, 1, 256, 2, 0)])
 @pytest.mark.parametrize("mode", ["direct", "graph"])
 def test_batch_strategies_match_oracle(ctx, chunks, expected, cfg, mode):
     modes, want = expected
     b = gpu.DeviceBatch(ctx, chunks)
     b.set_modes(modes)
-    b.set_tune(cfg[0], min_blocks=cfg[1], order=cfg[2])
+    b.set_tune(cfg[0], min_blocks=cfg[1], order=cfg[2], threads=cfg[3], grain=cfg[4], ctas=cfg[5])
     b.rebuild(LOD, mode=mode)
     b.finish()
     check_batch(b, modes, want)
@@ -83,7 +86,8 @@ def test_batch_autotune_picks_a_timed_config(ctx, chunks, expected):
     b = gpu.DeviceBatch(ctx, chunks)
     b.set_modes(modes)
     best, tried = b.autotune(LOD)
-    assert len(tried) >= 4 and all(t["ms"] > 0 for t in tried)
+    assert len(tried) >= 8 and all(t["ms"] > 0 for t in tried)
+    assert {t["threads"] for t in tried} == {256, 512} and {t["grain"] for t in tried} >= {1, 2, 4}
     assert best["ms"] == min(t["ms"] for t in tried)
     b.rebuild(LOD, mode="graph")
     b.finish()
@@ -107,3 +111,7 @@ def test_batch_rejects_bad_tunes(ctx, chunks):
         b.set_tune("split", order=0)
     with pytest.raises(gpu.VoxGpuError):
         b.set_tune("mixed", min_blocks=3)
+    with pytest.raises(gpu.VoxGpuError):
+        b.set_tune("mixed", threads=384)
+    with pytest.raises(gpu.VoxGpuError):
+        b.set_tune("mixed", grain=65)

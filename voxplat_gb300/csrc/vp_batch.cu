@@ -91,6 +91,8 @@ VP_API int vp_batch_create(vp_ctx *ctx, uint32_t n, const int *root_bitw, vp_bat
 	b->tune.order = 0;
 	b->tune.ctas = 0;
 	b->tune.ms = 0.f;
+	b->tune.threads = 512;
+	b->tune.grain = 1;
 	int rc;
 	if ((rc = dev_alloc(&b->d_off, n)) || (rc = dev_alloc(&b->d_len, n)) || (rc = dev_alloc(&b->d_sets, n)) ||
 	    (rc = dev_alloc(&b->d_items, n)) || (rc = dev_alloc(&b->d_outs, n)) || (rc = dev_alloc(&b->d_queue, 8)) ||
@@ -277,7 +279,8 @@ static GeoLaunch base_launch(vp_batch *b, int lod_max)
 	GeoLaunch L;
 	memset(&L, 0, sizeof(L));
 	L.sets = b->d_sets;
-	L.threads = 512;
+	L.threads = b->tune.threads ? b->tune.threads : 512u;
+	L.grain = b->tune.grain ? b->tune.grain : 1u;
 	L.outs = b->d_outs;
 	L.lod_max = lod_max;
 	L.big_scratch = b->d_big;
@@ -468,9 +471,32 @@ VP_API int vp_batch_set_tune(vp_batch *b, const vp_batch_tune *t)
 	if (t->strategy == VP_BATCH_SPLIT && t->order != 1) return VP_EINVAL; /* SPLIT needs root-grouped items */
 	if (t->min_blocks != 1 && t->min_blocks != 2) return VP_EINVAL;
 	if (b->big_slots && t->ctas > b->big_slots) return VP_EINVAL;
+	if (t->threads != 0 && t->threads != 256 && t->threads != 512) return VP_EINVAL;
+	if (t->grain > 64) return VP_EINVAL;
 	CK(cudaStreamSynchronize(b->ctx->stream));
 	b->tune = *t;
 	drop_graph(b);
+	return VP_OK;
+}
+
+/* Time one configuration: the first replay sizes the arenas and captures
+ * the graph, then `reps` replays are timed. */
+static int time_tune(vp_batch *b, int lod_max, vp_batch_tune *t, cudaEvent_t t0, cudaEvent_t t1)
+{
+	cudaStream_t st = b->ctx->stream;
+	int rc;
+	if ((rc = vp_batch_set_tune(b, t))) return rc;
+	if ((rc = enqueue_rebuild(b, lod_max, VP_REBUILD_GRAPH)) || (rc = vp_batch_finish(b))) return rc;
+	if ((rc = enqueue_rebuild(b, lod_max, VP_REBUILD_GRAPH))) return rc;
+	CK(cudaEventRecord(t0, st));
+	const int reps = 3;
+	for (int k = 0; k < reps; k++)
+		if ((rc = enqueue_rebuild(b, lod_max, VP_REBUILD_GRAPH))) return rc;
+	CK(cudaEventRecord(t1, st));
+	CK(cudaEventSynchronize(t1));
+	float ms = 0.f;
+	CK(cudaEventElapsedTime(&ms, t0, t1));
+	t->ms = ms / reps;
 	return VP_OK;
 }
 
@@ -478,50 +504,55 @@ VP_API int vp_batch_autotune(vp_batch *b, int lod_max, vp_batch_tune *best, vp_b
 {
 	if (!b || !b->uploaded || !best) return VP_EINVAL;
 	CK(cudaSetDevice(b->ctx->device));
-	const vp_batch_tune cand[] = {
-		{VP_BATCH_MIXED, 2, 0, 0, 0.f},
-		{VP_BATCH_MIXED, 2, 1, 0, 0.f},
-		{VP_BATCH_MIXED, 1, 0, 0, 0.f},
-		{VP_BATCH_SPLIT, 2, 1, 0, 0.f},
+	/* stage 1: strategy, order, register cap */
+	const vp_batch_tune stage1[] = {
+		{VP_BATCH_MIXED, 2, 0, 0, 0.f, 512, 1},
+		{VP_BATCH_MIXED, 2, 1, 0, 0.f, 512, 1},
+		{VP_BATCH_MIXED, 1, 0, 0, 0.f, 512, 1},
+		{VP_BATCH_SPLIT, 2, 1, 0, 0.f, 512, 1},
 	};
-	const int nc = (int)(sizeof(cand) / sizeof(cand[0]));
-	cudaStream_t st = b->ctx->stream;
 	cudaEvent_t t0, t1;
 	CK(cudaEventCreate(&t0));
 	CK(cudaEventCreate(&t1));
 	const int timing = b->ctx->timing;
 	b->ctx->timing = 0;
+	std::vector<vp_batch_tune> res;
 	int rc = VP_OK, bi = -1;
-	vp_batch_tune res[8];
-	for (int c = 0; c < nc && !rc; c++) {
-		res[c] = cand[c];
-		if ((rc = vp_batch_set_tune(b, &cand[c]))) break;
-		/* first replay sizes the arenas and captures the graph */
-		if ((rc = enqueue_rebuild(b, lod_max, VP_REBUILD_GRAPH)) || (rc = vp_batch_finish(b))) break;
-		if ((rc = enqueue_rebuild(b, lod_max, VP_REBUILD_GRAPH))) break;
-		cudaEventRecord(t0, st);
-		const int reps = 3;
-		for (int k = 0; k < reps && !rc; k++) rc = enqueue_rebuild(b, lod_max, VP_REBUILD_GRAPH);
-		cudaEventRecord(t1, st);
-		if (rc) break;
-		cudaError_t e = cudaEventSynchronize(t1);
-		if (e != cudaSuccess) {
-			rc = cuda_fail(e, "autotune sync");
-			break;
-		}
-		float ms = 0.f;
-		cudaEventElapsedTime(&ms, t0, t1);
-		res[c].ms = ms / reps;
-		if (bi < 0 || res[c].ms < res[bi].ms) bi = c;
+	for (const vp_batch_tune &c : stage1) {
+		vp_batch_tune t = c;
+		if ((rc = time_tune(b, lod_max, &t, t0, t1))) break;
+		res.push_back(t);
+		if (bi < 0 || t.ms < res[bi].ms) bi = (int)res.size() - 1;
+	}
+	/* stage 2: threads per chunk, chunks per dequeue and the persistent
+	 * grid around the best of stage 1 */
+	if (!rc) {
+		const vp_batch_tune base = res[bi];
+		const uint32_t sm = (uint32_t)b->ctx->sm_count;
+		for (uint32_t threads : {256u, 512u})
+			for (uint32_t grain : {1u, 2u, 4u})
+				for (uint32_t ctas : {0u, sm}) {
+					if (rc) break;
+					if (ctas && base.strategy != VP_BATCH_MIXED) continue;
+					if (threads == base.threads && grain == base.grain && ctas == base.ctas) continue;
+					if (b->big_slots && ctas > b->big_slots) continue;
+					vp_batch_tune t = base;
+					t.threads = threads;
+					t.grain = grain;
+					t.ctas = ctas;
+					if ((rc = time_tune(b, lod_max, &t, t0, t1))) break;
+					res.push_back(t);
+					if (t.ms < res[bi].ms) bi = (int)res.size() - 1;
+				}
 	}
 	b->ctx->timing = timing;
 	cudaEventDestroy(t0);
 	cudaEventDestroy(t1);
 	if (rc) return rc;
 	if (tried && ntried) {
-		const int m = std::min(*ntried, nc);
+		const int m = std::min(*ntried, (int)res.size());
 		for (int c = 0; c < m; c++) tried[c] = res[c];
-		*ntried = nc;
+		*ntried = (int)res.size();
 	}
 	*best = res[bi];
 	return vp_batch_set_tune(b, &res[bi]);

@@ -27,6 +27,8 @@ struct GeoLaunch {
 	 * passes it must shell every non-empty chunk whose geometry it builds. */
 	uint8_t *decoded;
 	const uint32_t *dec_slot;
+	/* persistent mixed and 128^3 launches: items per dequeue (0 = 1) */
+	uint32_t grain;
 };
 
 size_t geometry_smem_bytes(int root_bitw);

@@ -1333,31 +1333,36 @@ template <int MINB>
 __global__ void __launch_bounds__(512, MINB) k_geometry_mixed(const SetDesc *__restrict__ sets,
 							      const WorkItem *__restrict__ items, uint32_t nitems,
 							      unsigned int *queue, ChunkOut *outs, Arena asvl,
-							      Arena avbo, Arena aibo, int lod_max, uint8_t *scratch)
+							      Arena avbo, Arena aibo, int lod_max, uint8_t *scratch,
+							      uint32_t grain)
 {
 	extern __shared__ __align__(16) uint8_t smem[];
 	__shared__ uint32_t s_item;
 	uint32_t next = blockIdx.x;
 	for (;;) {
-		if (threadIdx.x == 0) s_item = queue ? atomicAdd(queue, 1u) : next;
+		/* `grain` consecutive items per dequeue */
+		if (threadIdx.x == 0) s_item = queue ? atomicAdd(queue, grain) : next;
 		__syncthreads();
-		const uint32_t it = s_item;
-		if (it >= nitems) break;
+		const uint32_t it0 = s_item;
+		if (it0 >= nitems) break;
 		next += gridDim.x;
-		const WorkItem wi = items[it];
-		const SetDesc S = sets[wi.set];
-		ChunkOut *out = outs + wi.slot;
-		switch (S.root_bitw) {
-		case 3: geometry_item<3>(S, wi, out, carve<3>(smem), asvl, avbo, aibo, lod_max); break;
-		case 4: geometry_item<4>(S, wi, out, carve<4>(smem), asvl, avbo, aibo, lod_max); break;
-		case 5: geometry_item<5>(S, wi, out, carve<5>(smem), asvl, avbo, aibo, lod_max); break;
-		case 6: geometry_item<6>(S, wi, out, carve<6>(smem), asvl, avbo, aibo, lod_max); break;
-		default: {
-			const Smem m6 = carve<6>(smem);
-			const BigMem bm = big_carve(scratch, blockIdx.x, m6.tmp, m6.nbr);
-			geometry_item_big(S, wi, out, bm, asvl, avbo, aibo, lod_max);
-			__syncthreads();
-		}
+		const uint32_t it1 = queue ? min(it0 + grain, nitems) : it0 + 1u;
+		for (uint32_t it = it0; it < it1; it++) {
+			const WorkItem wi = items[it];
+			const SetDesc S = sets[wi.set];
+			ChunkOut *out = outs + wi.slot;
+			switch (S.root_bitw) {
+			case 3: geometry_item<3>(S, wi, out, carve<3>(smem), asvl, avbo, aibo, lod_max); break;
+			case 4: geometry_item<4>(S, wi, out, carve<4>(smem), asvl, avbo, aibo, lod_max); break;
+			case 5: geometry_item<5>(S, wi, out, carve<5>(smem), asvl, avbo, aibo, lod_max); break;
+			case 6: geometry_item<6>(S, wi, out, carve<6>(smem), asvl, avbo, aibo, lod_max); break;
+			default: {
+				const Smem m6 = carve<6>(smem);
+				const BigMem bm = big_carve(scratch, blockIdx.x, m6.tmp, m6.nbr);
+				geometry_item_big(S, wi, out, bm, asvl, avbo, aibo, lod_max);
+				__syncthreads();
+			}
+			}
 		}
 	}
 }

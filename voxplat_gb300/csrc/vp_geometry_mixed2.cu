@@ -20,7 +20,8 @@ cudaError_t launch_geometry_mixed_b2(uint32_t grid, const GeoLaunch &L, cudaStre
 					     (int)Geo<6>::bytes);
 	if (e != cudaSuccess) return e;
 	k_geometry_mixed<2><<<grid, L.threads, Geo<6>::bytes, st>>>(L.sets, L.items, L.n_items, L.queue, L.outs, L.svl,
-								     L.vbo, L.ibo, L.lod_max, L.big_scratch);
+								     L.vbo, L.ibo, L.lod_max, L.big_scratch,
+								     L.grain ? L.grain : 1u);
 	return cudaGetLastError();
 }
 

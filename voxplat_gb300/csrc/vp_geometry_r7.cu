@@ -29,7 +29,7 @@ __global__ void __launch_bounds__(512, 1) k_shell_big(const SetDesc *__restrict_
 __global__ void __launch_bounds__(1024, 1) k_geometry_big(const SetDesc *__restrict__ sets,
 							 const WorkItem *__restrict__ items, uint32_t nitems,
 							 unsigned int *queue, ChunkOut *outs, Arena asvl, Arena avbo,
-							 Arena aibo, int lod_max, uint8_t *scratch)
+							 Arena aibo, int lod_max, uint8_t *scratch, uint32_t grain)
 {
 	__shared__ uint32_t tmp[64];
 	__shared__ int32_t nbr[28];
@@ -37,15 +37,19 @@ __global__ void __launch_bounds__(1024, 1) k_geometry_big(const SetDesc *__restr
 	const BigMem m = big_carve(scratch, blockIdx.x, tmp, nbr);
 	uint32_t next = blockIdx.x;
 	for (;;) {
-		if (threadIdx.x == 0) s_item = queue ? atomicAdd(queue, 1u) : next;
+		/* `grain` consecutive items per dequeue */
+		if (threadIdx.x == 0) s_item = queue ? atomicAdd(queue, grain) : next;
 		__syncthreads();
-		const uint32_t it = s_item;
-		if (it >= nitems) break;
+		const uint32_t it0 = s_item;
+		if (it0 >= nitems) break;
 		next += gridDim.x;
-		const WorkItem wi = items[it];
-		const SetDesc S = sets[wi.set];
-		geometry_item_big(S, wi, outs + wi.slot, m, asvl, avbo, aibo, lod_max);
-		__syncthreads();
+		const uint32_t it1 = queue ? min(it0 + grain, nitems) : it0 + 1u;
+		for (uint32_t it = it0; it < it1; it++) {
+			const WorkItem wi = items[it];
+			const SetDesc S = sets[wi.set];
+			geometry_item_big(S, wi, outs + wi.slot, m, asvl, avbo, aibo, lod_max);
+			__syncthreads();
+		}
 	}
 }
 
@@ -66,7 +70,7 @@ cudaError_t launch_big(const GeoLaunch &L, cudaStream_t st)
 		/* 1024 threads at 64 registers: twice the warps of the small path's
 		 * CTAs to hide the latency of the scratch, which lives in L2 */
 		k_geometry_big<<<grid, 1024, 0, st>>>(L.sets, L.items, L.n_items, L.queue, L.outs, L.svl, L.vbo, L.ibo,
-						    L.lod_max, L.big_scratch);
+						    L.lod_max, L.big_scratch, L.grain ? L.grain : 1u);
 		e = cudaGetLastError();
 	}
 	return e;

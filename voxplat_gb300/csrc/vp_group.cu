@@ -26,6 +26,8 @@
  * whole, and the host grows the arena and runs the rebuild and the grouping
  * again.
  */
+#include <algorithm>
+
 #include "vp_dev.cuh"
 #include "vp_group.h"
 
@@ -123,37 +125,44 @@ __global__ void k_group_level0(const ChunkOut *__restrict__ outs, uint32_t nchun
 	a.node_items[c] = outs[c].svl_items[0];
 }
 
-/* one CTA per (chunk, level >= 1): copy the chunk's level-l segment, one
- * splat (8 bytes) per thread per step; the first member of each node also
- * records the node's offset and length */
-__global__ void __launch_bounds__(256) k_group_copy(const ChunkOut *__restrict__ outs, uint32_t nchunks, GroupArgs a)
+/* levels >= 1: one warp per (chunk, level) segment, grid-stride: the warp
+ * copies the chunk's level-l segment to its node's place, one splat (8
+ * bytes) per lane per step; the first member of each node also records the
+ * node's offset and length. (A CTA per segment spent most of its time on
+ * launching CTAs for the many empty segments of worlds with air layers.) */
+__global__ void __launch_bounds__(256) k_group_copy(const ChunkOut *__restrict__ outs, uint32_t nchunks, int levels,
+						    GroupArgs a)
 {
-	const uint32_t c = blockIdx.x;
-	const int l = blockIdx.y + 1;
-	if (c >= nchunks) return;
+	const int lane = threadIdx.x & 31;
+	const uint64_t nseg = (uint64_t)nchunks * (uint64_t)levels;
+	const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
 	if (*a.svl_cursor > a.svl_cap_units) return; /* overflowed rebuild: rerun follows */
-	const GroupGeom g = group_geom(a.max_bitw, l);
-	uint32_t node, rank;
-	const uint32_t key = group_key(g, c, &node, &rank);
-	uint64_t lbase = 0;
-	for (int k = 1; k < l; k++) lbase += a.level_total[k];
-	const uint64_t *cnt = a.counts + (size_t)l * nchunks;
-	const uint64_t dst_off = lbase + cnt[key];
-	if (rank == 0 && threadIdx.x == 0) {
-		const uint32_t mbits = g.eb[0] + g.eb[1] + g.eb[2];
-		const uint32_t next_key = (node + 1u) << mbits;
-		const uint64_t end = next_key < nchunks ? cnt[next_key] : a.level_total[l];
-		a.node_off[(size_t)l * nchunks + node] = dst_off;
-		a.node_items[(size_t)l * nchunks + node] = (uint32_t)(end - cnt[key]);
+	for (uint64_t seg = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); seg < nseg; seg += nwarps) {
+		const int l = 1 + (int)(seg % (uint64_t)levels);
+		const uint32_t c = (uint32_t)(seg / (uint64_t)levels);
+		const GroupGeom g = group_geom(a.max_bitw, l);
+		uint32_t node, rank;
+		const uint32_t key = group_key(g, c, &node, &rank);
+		uint64_t lbase = 0;
+		for (int k = 1; k < l; k++) lbase += a.level_total[k];
+		const uint64_t *cnt = a.counts + (size_t)l * nchunks;
+		const uint64_t dst_off = lbase + cnt[key];
+		if (rank == 0 && lane == 0) {
+			const uint32_t mbits = g.eb[0] + g.eb[1] + g.eb[2];
+			const uint32_t next_key = (node + 1u) << mbits;
+			const uint64_t end = next_key < nchunks ? cnt[next_key] : a.level_total[l];
+			a.node_off[(size_t)l * nchunks + node] = dst_off;
+			a.node_items[(size_t)l * nchunks + node] = (uint32_t)(end - cnt[key]);
+		}
+		const uint32_t items = outs[c].svl_items[l];
+		if (!items) continue;
+		uint64_t src_off = outs[c].svl_off;
+		for (int k = 0; k < l; k++) src_off += outs[c].svl_items[k];
+		if (src_off + items > a.svl_cap_units * 8u || dst_off + items > a.out_cap) continue;
+		const uint2 *src = (const uint2 *)(a.svl + src_off);
+		uint2 *dst = (uint2 *)(a.out + dst_off);
+		for (uint32_t s = lane; s < items / 4u; s += 32u) dst[s] = __ldg(src + s);
 	}
-	const uint32_t items = outs[c].svl_items[l];
-	if (!items) return;
-	uint64_t src_off = outs[c].svl_off;
-	for (int k = 0; k < l; k++) src_off += outs[c].svl_items[k];
-	if (src_off + items > a.svl_cap_units * 8u || dst_off + items > a.out_cap) return;
-	const uint2 *src = (const uint2 *)(a.svl + src_off);
-	uint2 *dst = (uint2 *)(a.out + dst_off);
-	for (uint32_t s = threadIdx.x; s < items / 4u; s += blockDim.x) dst[s] = __ldg(src + s);
 }
 
 cudaError_t launch_group(const ChunkOut *outs, uint32_t nchunks, int lod_max, const GroupArgs &a, cudaStream_t st)
@@ -164,7 +173,10 @@ cudaError_t launch_group(const ChunkOut *outs, uint32_t nchunks, int lod_max, co
 	if (L > 1) {
 		k_group_scatter<<<dim3((nchunks + 255) / 256, L), 256, 0, st>>>(outs, nchunks, a);
 		k_group_scan<<<L, 1024, 0, st>>>(nchunks, a);
-		k_group_copy<<<dim3(nchunks, L - 1), 256, 0, st>>>(outs, nchunks, a);
+		/* 8 warps per CTA, up to 8 CTAs per SM of a 152-SM GPU */
+		const uint64_t nseg = (uint64_t)nchunks * (uint64_t)(L - 1);
+		const uint32_t grid = (uint32_t)std::min<uint64_t>((nseg + 7) / 8, 152u * 8u);
+		k_group_copy<<<grid, 256, 0, st>>>(outs, nchunks, L - 1, a);
 	}
 	return cudaGetLastError();
 }

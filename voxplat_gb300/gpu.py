@@ -50,12 +50,13 @@ assert EDIT_DTYPE.itemsize == 32
 
 class BatchTune(ctypes.Structure):
     _fields_ = [("strategy", ctypes.c_int), ("min_blocks", ctypes.c_int), ("order", ctypes.c_int),
-                ("ctas", ctypes.c_uint32), ("ms", ctypes.c_float)]
+                ("ctas", ctypes.c_uint32), ("ms", ctypes.c_float), ("threads", ctypes.c_uint32),
+                ("grain", ctypes.c_uint32)]
 
     def as_dict(self):
         return {"strategy": "mixed" if self.strategy == VP_BATCH_MIXED else "split", "min_blocks": self.min_blocks,
                 "order": "longest_first" if self.order == 0 else "by_root_then_longest", "ctas": self.ctas,
-                "ms": round(float(self.ms), 4)}
+                "threads": self.threads, "grain": self.grain, "ms": round(float(self.ms), 4)}
 
 
 class Camera(ctypes.Structure):
@@ -627,18 +628,20 @@ class DeviceBatch:
 
     def autotune(self, lod_max=4):
         best = BatchTune()
-        tried = (BatchTune * 8)()
-        n = ctypes.c_int(8)
+        tried = (BatchTune * 32)()
+        n = ctypes.c_int(32)
         check(self.lib.vp_batch_autotune(self.h, lod_max, ctypes.byref(best), tried, ctypes.byref(n)),
               "vp_batch_autotune")
         return best.as_dict(), [tried[i].as_dict() for i in range(n.value)]
 
-    def set_tune(self, strategy, min_blocks=2, order=None, ctas=0):
+    def set_tune(self, strategy, min_blocks=2, order=None, ctas=0, threads=512, grain=1):
         t = BatchTune()
         t.strategy = VP_BATCH_MIXED if strategy == "mixed" else VP_BATCH_SPLIT
         t.min_blocks = min_blocks
         t.order = (0 if t.strategy == VP_BATCH_MIXED else 1) if order is None else order
         t.ctas = ctas
+        t.threads = threads
+        t.grain = grain
         check(self.lib.vp_batch_set_tune(self.h, ctypes.byref(t)), "vp_batch_set_tune")
 
     def results(self):
