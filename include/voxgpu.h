@@ -309,6 +309,7 @@ VP_API int vp_rle_decode(vp_ctx *ctx, const uint32_t *words, uint32_t nwords, ui
  * that chunk. */
 #define VP_STATUS_OVERFLOW 1u   /* vp_chunk_result.status: output arena too small */
 #define VP_STATUS_BAD_STREAM 2u /* vp_chunk_result.status: the chunk's stream failed the check */
+#define VP_STATUS_TIMEOUT 4u    /* vp_chunk_result.status: a bounded device wait for its data ran out */
 VP_API int vp_rebuild_noalloc(int device, void *stream, int root_bitw, const int max_bitw[3], const uint32_t *pool,
 			      uint64_t pool_words, const uint64_t *off, const uint32_t *len, const uint16_t *shadow,
 			      uint64_t shadow_len, uint32_t shadow_w, const uint8_t *make_mesh, int lod_max,

@@ -61,7 +61,7 @@ struct ChunkOut {
 	uint32_t status;     /* 0 ok, else a kStatus* bit set */
 };
 
-enum : uint32_t { kStatusOverflow = 1u, kStatusBadStream = 2u };
+enum : uint32_t { kStatusOverflow = 1u, kStatusBadStream = 2u, kStatusTimeout = 4u };
 
 /* no slot (handoff table of decoded chunks) */
 constexpr uint32_t kNoSlot = 0xFFFFFFFFu;

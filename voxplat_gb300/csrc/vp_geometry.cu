@@ -55,7 +55,13 @@ size_t shell_cols_per_chunk(int root_bitw) { return 3u * (1u << root_bitw) * (1u
 
 size_t decoded_bytes_per_chunk(int root_bitw)
 {
-	return root_bitw >= 3 && root_bitw <= 6 ? (size_t)(1u << (2 * root_bitw)) * 20u : 0u;
+	switch (root_bitw) {
+	case 3: return Geo<3>::dec_bytes;
+	case 4: return Geo<4>::dec_bytes;
+	case 5: return Geo<5>::dec_bytes;
+	case 6: return Geo<6>::dec_bytes;
+	default: return 0; /* 128^3 chunks are not handed over */
+	}
 }
 
 cudaError_t launch_geometry(int root_bitw, const GeoLaunch &L, cudaStream_t st)

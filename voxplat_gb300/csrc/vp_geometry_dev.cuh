@@ -75,7 +75,8 @@ struct Geo {
 	static constexpr size_t bytes = a16(o_nbr + sizeof(int32_t) * 28);
 	/* a decoded chunk handed from the shell pass to the geometry pass:
 	 * occupancy rows and run-start rows (u64, row r = z R + y), then ranks */
-	static constexpr size_t dec_bytes = (size_t)RR * (8 + 8 + 4);
+	static constexpr size_t dec_occ = (size_t)R * H * 8;  /* z planes 0..R-1, halo rows included */
+	static constexpr size_t dec_bytes = dec_occ + (size_t)RR * (8 + 4);
 	static constexpr size_t shell_words = 6 * R;   /* u64 per chunk */
 	static constexpr size_t shell_cols = 3 * RR;   /* bytes per chunk */
 };
@@ -281,51 +282,93 @@ __device__ __forceinline__ uint32_t colour_at(const uint32_t *__restrict__ s, co
 	return __ldg(s + run) >> 24;
 }
 
-/* The decoded chunk (occupancy rows without halo, run-start rows, ranks)
- * to global memory, and back: the shell pass decodes every chunk anyway,
- * so the geometry pass of the same rebuild loads instead of decoding. */
-template <int RB>
-__device__ void store_decoded(const Smem &m, uint8_t *dst)
-{
-	using G = Geo<RB>;
-	constexpr int R = G::R, RR = G::RR;
-	uint64_t *occ = (uint64_t *)dst;
-	uint4 *rs = (uint4 *)(dst + (size_t)RR * 8);
-	uint4 *rank = (uint4 *)(dst + (size_t)RR * 16);
-	for (int r = threadIdx.x; r < RR; r += blockDim.x) occ[r] = m.occ[hidx<RB>(r & (R - 1), r >> RB)];
-	for (int i = threadIdx.x; i < RR / 2; i += blockDim.x) rs[i] = ((const uint4 *)m.rs)[i];
-	for (int i = threadIdx.x; i < RR / 4; i += blockDim.x) rank[i] = ((const uint4 *)m.rank)[i];
-}
-
-/* 8- and 16-byte asynchronous global -> shared copies (cp.async): every
- * thread has all of its copies in flight at once. */
-__device__ __forceinline__ void copy_async8(void *dst, const void *src)
-{
-	asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
-		     "l"(src)
-		     : "memory");
-}
-
-__device__ __forceinline__ void copy_async16(void *dst, const void *src)
-{
-	asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
-		     "l"(src)
-		     : "memory");
-}
+/* The decoded chunk handed from the shell pass to the geometry pass of the
+ * same rebuild: the occupancy planes z = 0..R-1 as they lie in shared
+ * memory (R+2 rows each, halo rows included; the geometry pass rewrites
+ * those in load_halo), the run-start rows and the ranks. Both directions
+ * are 1-D bulk copies (cp.async.bulk): three per chunk, issued by one
+ * thread; every block starts on a 16-byte boundary and is a multiple of 16
+ * bytes long. */
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 template <int RB>
-__device__ void load_decoded(const uint8_t *src, const Smem &m)
+__device__ __forceinline__ void store_decoded(const Smem &m, uint8_t *dst)
 {
 	using G = Geo<RB>;
-	constexpr int R = G::R, RR = G::RR;
-	const uint64_t *occ = (const uint64_t *)src;
-	const uint4 *rs = (const uint4 *)(src + (size_t)RR * 8);
-	const uint4 *rank = (const uint4 *)(src + (size_t)RR * 16);
-	for (int r = threadIdx.x; r < RR; r += blockDim.x) copy_async8(m.occ + hidx<RB>(r & (R - 1), r >> RB), occ + r);
-	for (int i = threadIdx.x; i < RR / 2; i += blockDim.x) copy_async16((uint4 *)m.rs + i, rs + i);
-	for (int i = threadIdx.x; i < RR / 4; i += blockDim.x) copy_async16((uint4 *)m.rank + i, rank + i);
-	asm volatile("cp.async.wait_all;\n" ::: "memory");
+	static_assert(G::dec_occ % 16 == 0 && (G::RR * 8) % 16 == 0 && (G::RR * 4) % 16 == 0, "bulk copy sizes");
+	static_assert((G::o_occ + G::H * 8) % 16 == 0 && G::o_rs % 16 == 0 && G::o_rank % 16 == 0, "bulk copy bases");
+	__syncthreads(); /* the decode's shared-memory writes, then the async proxy reads them */
+	if (threadIdx.x == 0) {
+		asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+		asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n" ::"l"(dst),
+			     "r"(smem_u32(m.occ + G::H)), "r"((uint32_t)G::dec_occ)
+			     : "memory");
+		asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n" ::"l"(dst + G::dec_occ),
+			     "r"(smem_u32(m.rs)), "r"((uint32_t)(G::RR * 8))
+			     : "memory");
+		asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n" ::"l"(
+				     dst + G::dec_occ + G::RR * 8),
+			     "r"(smem_u32(m.rank)), "r"((uint32_t)(G::RR * 4))
+			     : "memory");
+		asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+	}
+}
+
+/* The bulk stores must have read shared memory before the next decode
+ * overwrites it, and be complete before the kernel ends (no user spin: the
+ * hardware wait instruction). */
+__device__ __forceinline__ void store_decoded_wait()
+{
+	if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
+}
+
+/* Bounded wait on the mbarrier's phase; false when it ran out. */
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t phase)
+{
+	for (uint32_t tries = 0; tries < (1u << 16); tries++) {
+		uint32_t ok;
+		asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+			     " selp.u32 %0, 1, 0, p;\n}\n"
+			     : "=r"(ok)
+			     : "r"(smem_u32(bar)), "r"(phase)
+			     : "memory");
+		if (ok) return true;
+	}
+	return false;
+}
+
+/* Loads a decoded chunk with three bulk copies completing on `bar` (phase
+ * `phase`). Returns false on every thread when they did not arrive within
+ * the bounded wait (the flag is set). */
+template <int RB>
+__device__ bool load_decoded(const uint8_t *src, const Smem &m, uint64_t *bar, uint32_t phase, uint32_t *flag)
+{
+	using G = Geo<RB>;
+	if (threadIdx.x == 0) {
+		/* earlier generic accesses to these bytes come before the copies */
+		asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+		asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)),
+			     "r"((uint32_t)G::dec_bytes)
+			     : "memory");
+		asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+				     smem_u32(m.occ + G::H)),
+			     "l"(src), "r"((uint32_t)G::dec_occ), "r"(smem_u32(bar))
+			     : "memory");
+		asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+				     smem_u32(m.rs)),
+			     "l"(src + G::dec_occ), "r"((uint32_t)(G::RR * 8)), "r"(smem_u32(bar))
+			     : "memory");
+		asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+				     smem_u32(m.rank)),
+			     "l"(src + G::dec_occ + G::RR * 8), "r"((uint32_t)(G::RR * 4)), "r"(smem_u32(bar))
+			     : "memory");
+	}
+	const bool ok = mbar_wait(bar, phase);
+	if (!ok) atomicOr(flag, 1u);
 	__syncthreads();
+	const bool all = *flag == 0u;
+	__syncthreads();
+	return all;
 }
 
 /* ------------------------------------------------------------------ */
@@ -348,10 +391,8 @@ __global__ void __launch_bounds__(512, 2) k_shell(const SetDesc *__restrict__ se
 	if (chunk_is_null(S, wi.chunk, N)) return;
 	const uint32_t *stream = S.pool + S.off[wi.chunk];
 	decode_chunk<RB>(stream, S.len[wi.chunk] - 1u, m);
-	if (decoded) {
-		const uint32_t ds = dec_slot[wi.chunk];
-		if (ds != kNoSlot) store_decoded<RB>(m, decoded + (size_t)ds * G::dec_bytes);
-	}
+	const uint32_t ds = decoded ? dec_slot[wi.chunk] : kNoSlot;
+	if (ds != kNoSlot) store_decoded<RB>(m, decoded + (size_t)ds * G::dec_bytes);
 	uint64_t *bits = S.shell_bits + (size_t)wi.chunk * G::shell_words;
 	uint8_t *cols = S.shell_col + (size_t)wi.chunk * G::shell_cols;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -389,6 +430,7 @@ __global__ void __launch_bounds__(512, 2) k_shell(const SetDesc *__restrict__ se
 		cols[RR + i] = (uint8_t)c1;
 		cols[2 * RR + i] = (uint8_t)c2;
 	}
+	if (ds != kNoSlot) store_decoded_wait();
 }
 
 /* ------------------------------------------------------------------ */
@@ -1257,7 +1299,8 @@ __device__ void mask_dense(const SetDesc &S, const uint32_t *__restrict__ stream
 template <int RB>
 __device__ __forceinline__ void geometry_item(const SetDesc &S, const WorkItem &wi, ChunkOut *out, const Smem &m,
 					      const Arena &asvl, const Arena &avbo, const Arena &aibo, int lod_max,
-					      const uint8_t *decoded = nullptr, const uint32_t *dec_slot = nullptr)
+					      const uint8_t *decoded = nullptr, const uint32_t *dec_slot = nullptr,
+					      uint64_t *bar = nullptr, uint32_t *phase = nullptr, uint32_t *flag = nullptr)
 {
 	using G = Geo<RB>;
 	constexpr int R = G::R;
@@ -1283,10 +1326,19 @@ __device__ __forceinline__ void geometry_item(const SetDesc &S, const WorkItem &
 	const uint32_t *stream = S.pool + S.off[wi.chunk];
 	/* the shell pass of this rebuild stored every chunk but the all-air ones */
 	const uint32_t ds = decoded && !chunk_is_null(S, wi.chunk, N) ? dec_slot[wi.chunk] : kNoSlot;
-	if (ds != kNoSlot)
-		load_decoded<RB>(decoded + (size_t)ds * G::dec_bytes, m);
-	else
+	if (ds != kNoSlot) {
+		if (!load_decoded<RB>(decoded + (size_t)ds * G::dec_bytes, m, bar, *phase, flag)) {
+			/* the copies did not arrive: one more bounded wait for them,
+			 * then report the chunk; the CTA stops */
+			mbar_wait(bar, *phase);
+			if (threadIdx.x == 0) out->status = kStatusTimeout;
+			__syncthreads();
+			return;
+		}
+		*phase ^= 1u;
+	} else {
 		decode_chunk<RB>(stream, S.len[wi.chunk] - 1u, m);
+	}
 	load_halo<RB>(S, m);
 	if (wi.flags & kItemMaskDense)
 		mask_dense<RB>(S, stream, m, (uint8_t *)asvl.base + (size_t)wi.slot * G::S * G::S * G::S);
@@ -1306,16 +1358,26 @@ __global__ void __launch_bounds__(512, 2) k_geometry(const SetDesc *__restrict__
 	extern __shared__ __align__(16) uint8_t smem[];
 	const Smem m = carve<RB>(smem);
 	__shared__ uint32_t s_item;
+	__shared__ __align__(8) uint64_t s_bar; /* completion of the decoded-chunk bulk copies */
+	__shared__ uint32_t s_flag;             /* a bounded wait ran out */
+	uint32_t phase = 0;
+	if (threadIdx.x == 0) {
+		asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_bar)) : "memory");
+		asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+		s_flag = 0u;
+	}
+	__syncthreads();
 	uint32_t next = blockIdx.x;
 	for (;;) {
 		if (threadIdx.x == 0) s_item = queue ? atomicAdd(queue, 1u) : next;
 		__syncthreads();
 		const uint32_t it = s_item;
-		if (it >= nitems) break;
+		if (it >= nitems || s_flag) break;
 		next = nitems;
 		const WorkItem wi = items[it];
 		const SetDesc S = sets[wi.set];
-		geometry_item<RB>(S, wi, outs + wi.slot, m, asvl, avbo, aibo, lod_max, decoded, dec_slot);
+		geometry_item<RB>(S, wi, outs + wi.slot, m, asvl, avbo, aibo, lod_max, decoded, dec_slot, &s_bar, &phase,
+				  &s_flag);
 	}
 }
 
