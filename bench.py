@@ -304,6 +304,23 @@ def run_ours(args):
         torch.cuda.synchronize()
         plain_ms.append(a_.elapsed_time(b_))
     plain_value = world.nchunks / (float(np.median(plain_ms)) / 1e3)
+    # the same launches spread over 16 streams, so they run side by side
+    dw.rebuild(LOD_MAX, persistent=False, concurrent=True)
+    dw.finish()
+    conc_ms = []
+    for _ in range(2):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            a_ = torch.cuda.Event(enable_timing=True)
+            b_ = torch.cuda.Event(enable_timing=True)
+            a_.record(stream)
+        dw.rebuild(LOD_MAX, persistent=False, concurrent=True)
+        with torch.cuda.stream(stream):
+            b_.record(stream)
+        ctx.sync()
+        torch.cuda.synchronize()
+        conc_ms.append(a_.elapsed_time(b_))
+    plain_conc_value = world.nchunks / (float(np.median(conc_ms)) / 1e3)
     # end to end through the C ABI with host buffers: the caller's world and
     # its output buffers live in pinned host memory; every step uploads the
     # world (H2D + device validation), rebuilds, and reads the result
@@ -407,12 +424,16 @@ def run_ours(args):
         "kernel_ms": {"shell": round(shell_ms / args.steps, 4), "geometry": round(geo_avg_ms, 4),
                       "group": round(grp_ms / args.steps, 4)},
         "plain_value": round(plain_value, 1),
+        "plain_concurrent_value": round(plain_conc_value, 1),
         "gpu_launches": int(launches),
     }
     detail = {"detail": "bench.py sub-benchmarks; the headline is the next line",
               "voxels_per_s": round(value * world.R ** 3, 1),
               "plain": {"value": round(plain_value, 1), "unit": "chunks/s", "launches_per_step": 2 * world.nchunks,
-                        "batched_over_plain": round(value / plain_value, 2)},
+                        "batched_over_plain": round(value / plain_value, 2),
+                        "concurrent": {"value": round(plain_conc_value, 1), "streams": 16,
+                                       "batched_over_plain": round(value / plain_conc_value, 2),
+                                       "note": "the same launches round-robin over 16 streams"}},
               "e2e": {"steps": n_e2e, "ms_per_step": round(e2e_ms, 3),
                       "path": "pinned host world -> vp_world_upload -> vp_world_rebuild_to_host_async (group; "
                               "outputs stream back per slab, and under the next step's upload and compute) -> two "
@@ -442,6 +463,7 @@ def run_ours(args):
             ub = uneven_batch(ctx)
             detail["uneven_batch"] = ub
             out["uneven_batched_over_plain"] = ub["batched_over_plain"]
+            out["uneven_batched_over_plain_concurrent"] = ub["batched_over_plain_concurrent"]
         if not args.skip_full_scale:
             fs = full_scale(ctx)
             res5, dw5 = fs.pop("_res"), fs.pop("_dw")
@@ -514,6 +536,9 @@ def uneven_batch(ctx, n=4096, seed=3, steps=5):
     b.rebuild(LOD_MAX, mode="plain")
     b.finish()
     p_ms, p_launches = b.kernel_ms()
+    b.rebuild(LOD_MAX, mode="concurrent")
+    b.finish()
+    c_ms, _ = b.kernel_ms()
     ctx.set_timing(False)
     res = b.results()
     out_b = int(res["svl_total"].astype(np.int64).sum()) * 2
@@ -532,6 +557,8 @@ def uneven_batch(ctx, n=4096, seed=3, steps=5):
         "plain_chunks_per_s": round(n / (p_ms / 1e3), 1),
         "plain_launches_per_rebuild": p_launches,
         "batched_over_plain": round(p_ms / g_ms, 2),
+        "plain_concurrent_ms": round(c_ms, 3),
+        "batched_over_plain_concurrent": round(c_ms / g_ms, 2),
         "tune": best,
         "tried": tried,
         "rle_in_mb": round(b.rle_bytes / 1e6, 1),

@@ -70,6 +70,7 @@ typedef struct vp_chunk_result {
 #define VP_REBUILD_PLAIN 2u      /* one launch per chunk and pass (comparison path) */
 #define VP_REBUILD_GROUP 4u      /* also build the LOD/octree draw groups */
 #define VP_REBUILD_GRAPH 8u      /* batches: replay the tuned configuration's CUDA graph */
+#define VP_REBUILD_CONCURRENT 16u /* one launch per chunk and pass, spread over 16 streams (comparison path) */
 
 VP_API const char *vp_strerror(int code);
 VP_API const char *vp_last_cuda_error(void);

@@ -72,11 +72,12 @@ def test_batch_strategies_match_oracle(ctx, chunks, expected, cfg, mode):
         check_batch(b, modes, want)
 
 
-def test_batch_plain_matches_oracle(ctx, chunks, expected):
+@pytest.mark.parametrize("mode", ["plain", "concurrent"])
+def test_batch_plain_matches_oracle(ctx, chunks, expected, mode):
     modes, want = expected
     b = gpu.DeviceBatch(ctx, chunks)
     b.set_modes(modes)
-    b.rebuild(LOD, mode="plain")
+    b.rebuild(LOD, mode=mode)
     b.finish()
     check_batch(b, modes, want)
 

@@ -46,7 +46,8 @@ def test_group_matches_oracle(ctx, root_bitw, max_bitw, lod_max):
                     assert np.array_equal(got, want), (lod, nx, ny, nz)
 
 
-def test_plain_path_matches_batched(ctx):
+@pytest.mark.parametrize("concurrent", [False, True])
+def test_plain_path_matches_batched(ctx, concurrent):
     w = worlds.cave_world(5, (1, 2, 1), seed=77)
     dw = gpu.DeviceWorld(ctx, w)
     modes = (np.arange(w.nchunks) % 2).astype(np.uint8)
@@ -55,7 +56,7 @@ def test_plain_path_matches_batched(ctx):
     dw.finish()
     a = dw.results()
     ref = {c: (dw.chunk_mesh(a, c) if modes[c] else dw.chunk_splats(a, c)[0]) for c in range(w.nchunks)}
-    dw.rebuild(lod_max=4, persistent=False, plain=True)
+    dw.rebuild(lod_max=4, persistent=False, plain=not concurrent, concurrent=concurrent)
     dw.finish()
     b = dw.results()
     for c in range(w.nchunks):

@@ -266,6 +266,7 @@ VP_API void vp_world_destroy(vp_world *w)
 		cudaStreamSynchronize(w->copy_stream);
 		cudaStreamDestroy(w->copy_stream);
 	}
+	vpi_plain_free(w->plain);
 	for (int h = 0; h < 2; h++)
 		if (w->half_done[h]) cudaEventDestroy(w->half_done[h]);
 	if (w->outs_alt[1]) {
@@ -291,6 +292,44 @@ VP_API void vp_world_destroy(vp_world *w)
 	vpi_edit_state_free(w);
 	for (cudaEvent_t e : w->ev) cudaEventDestroy(e);
 	delete w;
+}
+
+int vpi_plain_fork(PlainStreams &p, cudaStream_t main)
+{
+	if (!p.fork) {
+		for (int k = 0; k < kPlainStreams; k++) {
+			CK(cudaStreamCreateWithFlags(&p.s[k], cudaStreamNonBlocking));
+			CK(cudaEventCreateWithFlags(&p.ev[k], cudaEventDisableTiming));
+		}
+		CK(cudaEventCreateWithFlags(&p.fork, cudaEventDisableTiming));
+	}
+	CK(cudaEventRecord(p.fork, main));
+	for (int k = 0; k < kPlainStreams; k++) CK(cudaStreamWaitEvent(p.s[k], p.fork, 0));
+	return VP_OK;
+}
+
+int vpi_plain_join(PlainStreams &p, cudaStream_t main)
+{
+	for (int k = 0; k < kPlainStreams; k++) {
+		CK(cudaEventRecord(p.ev[k], p.s[k]));
+		CK(cudaStreamWaitEvent(main, p.ev[k], 0));
+	}
+	return VP_OK;
+}
+
+void vpi_plain_free(PlainStreams &p)
+{
+	for (int k = 0; k < kPlainStreams; k++) {
+		if (p.s[k]) {
+			cudaStreamSynchronize(p.s[k]);
+			cudaStreamDestroy(p.s[k]);
+		}
+		if (p.ev[k]) cudaEventDestroy(p.ev[k]);
+		p.s[k] = nullptr;
+		p.ev[k] = nullptr;
+	}
+	if (p.fork) cudaEventDestroy(p.fork);
+	p.fork = nullptr;
 }
 
 int vpi_validate_stream(const uint32_t *s, uint32_t n, uint64_t N)
@@ -724,17 +763,26 @@ static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 		cudaEventRecord(e0, st);
 	}
 	cudaError_t e = cudaSuccess;
-	if (flags & VP_REBUILD_PLAIN) {
+	if (flags & (VP_REBUILD_PLAIN | VP_REBUILD_CONCURRENT)) {
 		/* one launch per chunk and pass: every shell, then every chunk's
-		 * geometry (a chunk reads its neighbours' shells) */
+		 * geometry (a chunk reads its neighbours' shells); on the context
+		 * stream, or round-robin over forked streams */
+		const bool conc = (flags & VP_REBUILD_CONCURRENT) != 0;
+		if (conc && (rc = vpi_plain_fork(w->plain, st))) return rc;
 		for (uint32_t k = 0; k < w->nchunks && e == cudaSuccess; k++) {
 			GeoLaunch Ls = L;
 			Ls.n_items = 0;
 			Ls.shell_items = w->d_items + k;
 			Ls.n_shell = 1;
 			Ls.run_shell = 1;
-			e = launch_geometry(w->root_bitw, Ls, st);
+			if (conc && w->root_bitw == 7) { /* a scratch slot per stream */
+				Ls.big_scratch = w->d_big + (size_t)(k % kPlainStreams) * big_scratch_slot_bytes();
+				Ls.big_slots = 1;
+			}
+			e = launch_geometry(w->root_bitw, Ls, conc ? w->plain.s[k % kPlainStreams] : st);
 		}
+		if (conc && e == cudaSuccess && ((rc = vpi_plain_join(w->plain, st)) || (rc = vpi_plain_fork(w->plain, st))))
+			return rc;
 		if (ctx->timing) cudaEventRecord(e1, st);
 		for (uint32_t k = 0; k < w->nchunks && e == cudaSuccess; k++) {
 			GeoLaunch Lg = L;
@@ -742,9 +790,14 @@ static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 			Lg.items = w->d_items + k;
 			Lg.n_items = 1;
 			Lg.queue = nullptr;
-			e = launch_geometry(w->root_bitw, Lg, st);
+			if (conc && w->root_bitw == 7) {
+				Lg.big_scratch = w->d_big + (size_t)(k % kPlainStreams) * big_scratch_slot_bytes();
+				Lg.big_slots = 1;
+			}
+			e = launch_geometry(w->root_bitw, Lg, conc ? w->plain.s[k % kPlainStreams] : st);
 		}
 		if (e != cudaSuccess) return cuda_fail(e, "plain launches");
+		if (conc && (rc = vpi_plain_join(w->plain, st))) return rc;
 		w->launches += 2 * w->nchunks;
 	} else {
 		L.run_shell = 1;
@@ -1282,7 +1335,7 @@ VP_API int vp_world_rebuild_to_host(vp_world *w, int lod_max, unsigned flags, in
 {
 	if (!w || !w->uploaded || !results || !used_bytes) return VP_EINVAL;
 	if (lod_max < 0 || lod_max >= VP_MAX_LEVELS || slabs < 1 || slabs > kMaxStreamSlabs) return VP_EINVAL;
-	if ((flags & VP_REBUILD_PLAIN) || w->root_bitw == 7) {
+	if ((flags & (VP_REBUILD_PLAIN | VP_REBUILD_CONCURRENT)) || w->root_bitw == 7) {
 		/* per-chunk launches and 128^3 chunks take the plain sequence */
 		int rc;
 		if ((rc = vp_world_rebuild(w, lod_max, flags)) || (rc = vp_world_finish(w)) ||
@@ -1300,7 +1353,7 @@ VP_API int vp_world_rebuild_to_host_async(vp_world *w, int lod_max, unsigned fla
 {
 	if (!w || !w->uploaded || !results || !used_bytes) return VP_EINVAL;
 	if (lod_max < 0 || lod_max >= VP_MAX_LEVELS || slabs < 1 || slabs > kMaxStreamSlabs) return VP_EINVAL;
-	if ((flags & VP_REBUILD_PLAIN) || w->root_bitw == 7)
+	if ((flags & (VP_REBUILD_PLAIN | VP_REBUILD_CONCURRENT)) || w->root_bitw == 7)
 		return vp_world_rebuild_to_host(w, lod_max, flags, slabs, svl, svl_bytes, vbo, vbo_bytes, ibo, ibo_bytes,
 						results, used_bytes);
 	return stream_rebuild(w, lod_max, flags, slabs, svl, svl_bytes, vbo, vbo_bytes, ibo, ibo_bytes, results,

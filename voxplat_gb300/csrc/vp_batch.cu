@@ -58,6 +58,7 @@ struct vp_batch {
 	cudaGraphExec_t gexec = nullptr;
 	int graph_lod = -1;
 	cudaStream_t side[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+	PlainStreams plain;              /* VP_REBUILD_CONCURRENT */
 	cudaEvent_t fork = nullptr, join[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 	/* timing */
 	std::vector<cudaEvent_t> ev;
@@ -137,6 +138,7 @@ VP_API void vp_batch_destroy(vp_batch *b)
 		if (b->join[i]) cudaEventDestroy(b->join[i]);
 	}
 	if (b->fork) cudaEventDestroy(b->fork);
+	vpi_plain_free(b->plain);
 	for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
 	dev_free(b->d_pool);
 	dev_free(b->d_off);
@@ -336,18 +338,30 @@ static int enqueue_batched(vp_batch *b, int lod_max, cudaStream_t st)
 	return VP_OK;
 }
 
-static int enqueue_plain(vp_batch *b, int lod_max, cudaStream_t st)
+/* One launch per chunk, on `st` or (conc) round-robin over forked streams;
+ * a 128^3 chunk then uses the scratch slot of its stream, so two of them
+ * never share a slot. */
+static int enqueue_plain(vp_batch *b, int lod_max, cudaStream_t st, bool conc)
 {
 	CK(cudaMemsetAsync(b->d_cursors, 0, 3 * sizeof(unsigned long long), st));
 	GeoLaunch L = base_launch(b, lod_max);
+	int rc;
+	if (conc && (rc = vpi_plain_fork(b->plain, st))) return rc;
 	for (uint32_t i = 0; i < b->n; i++) {
 		GeoLaunch G = L;
 		G.items = b->d_items + i;
 		G.n_items = 1;
 		G.queue = nullptr;
-		cudaError_t e = launch_geometry(b->rb[b->items[i].set], G, st);
+		const int k = (int)(i % kPlainStreams);
+		const int rb = b->rb[b->items[i].set];
+		if (conc && rb == 7) {
+			G.big_scratch = b->d_big + (size_t)k * big_scratch_slot_bytes();
+			G.big_slots = 1;
+		}
+		cudaError_t e = launch_geometry(rb, G, conc ? b->plain.s[k] : st);
 		if (e != cudaSuccess) return cuda_fail(e, "plain launch");
 	}
+	if (conc && (rc = vpi_plain_join(b->plain, st))) return rc;
 	b->launches += b->n;
 	return VP_OK;
 }
@@ -386,7 +400,8 @@ static int enqueue_rebuild(vp_batch *b, int lod_max, unsigned flags)
 	cudaStream_t st = ctx->stream;
 	int rc;
 	if ((rc = ensure_arenas(b))) return rc;
-	if (!(flags & VP_REBUILD_PLAIN) && b->items_order != b->tune.order) {
+	const bool plain = (flags & (VP_REBUILD_PLAIN | VP_REBUILD_CONCURRENT)) != 0;
+	if (!plain && b->items_order != b->tune.order) {
 		drop_graph(b);
 		if ((rc = upload_items(b, b->tune.order))) return rc;
 	}
@@ -396,8 +411,8 @@ static int enqueue_rebuild(vp_batch *b, int lod_max, unsigned flags)
 		cudaEventCreate(&e1);
 		cudaEventRecord(e0, st);
 	}
-	if (flags & VP_REBUILD_PLAIN) {
-		rc = enqueue_plain(b, lod_max, st);
+	if (plain) {
+		rc = enqueue_plain(b, lod_max, st, (flags & VP_REBUILD_CONCURRENT) != 0);
 	} else if (flags & VP_REBUILD_GRAPH) {
 		if (!b->gexec || b->graph_lod != lod_max) rc = capture_graph(b, lod_max);
 		if (!rc) {

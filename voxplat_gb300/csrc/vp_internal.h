@@ -50,6 +50,19 @@ struct vp_ctx {
 
 constexpr int kMaxStreamSlabs = 16;
 
+/* Streams for the concurrent plain comparison path: one launch per chunk,
+ * spread round-robin over kPlainStreams streams forked from and joined back
+ * into the caller's stream. */
+constexpr int kPlainStreams = 16;
+struct PlainStreams {
+	cudaStream_t s[kPlainStreams] = {};
+	cudaEvent_t ev[kPlainStreams] = {};
+	cudaEvent_t fork = nullptr;
+};
+extern "C" int vpi_plain_fork(PlainStreams &p, cudaStream_t main); /* creates the streams on first use */
+extern "C" int vpi_plain_join(PlainStreams &p, cudaStream_t main);
+extern "C" void vpi_plain_free(PlainStreams &p);
+
 struct EditSlot; /* one edit batch's device buffers, stream and bookkeeping (vp_serve.cu) */
 
 struct vp_world {
@@ -143,6 +156,7 @@ struct vp_world {
 	std::vector<int32_t> slot_of;            /* chunk -> volume slot while a batch is planned */
 	std::vector<uint32_t> last_dirty;
 	uint64_t shadow_base = 0;                /* world index of d_shadow[0] */
+	PlainStreams plain;                      /* VP_REBUILD_CONCURRENT */
 	std::vector<cudaEvent_t> ev;             /* pairs per kernel */
 	std::vector<int> ev_kind;                /* 0 shell, 1 geometry */
 	double ms[3] = {0, 0, 0};

@@ -16,6 +16,7 @@ VP_REBUILD_PERSISTENT = 1
 VP_REBUILD_PLAIN = 2
 VP_REBUILD_GROUP = 4
 VP_REBUILD_GRAPH = 8
+VP_REBUILD_CONCURRENT = 16
 VP_BATCH_MIXED = 0
 VP_BATCH_SPLIT = 1
 
@@ -331,9 +332,11 @@ class DeviceWorld:
             assert len(m) == self.nchunks
             check(self.lib.vp_world_set_modes(self.h, _p(m)), "vp_world_set_modes")
 
-    def rebuild(self, lod_max=4, persistent=True, plain=False, group=False):
+    def rebuild(self, lod_max=4, persistent=True, plain=False, group=False, concurrent=False):
+        """plain: one launch per chunk and pass on the context stream;
+        concurrent: the same launches spread over 16 streams."""
         flags = (VP_REBUILD_PERSISTENT if persistent else 0) | (VP_REBUILD_PLAIN if plain else 0) \
-            | (VP_REBUILD_GROUP if group else 0)
+            | (VP_REBUILD_GROUP if group else 0) | (VP_REBUILD_CONCURRENT if concurrent else 0)
         check(self.lib.vp_world_rebuild(self.h, lod_max, flags), "vp_world_rebuild")
 
     def group_nodes(self, lod):
@@ -618,9 +621,11 @@ class DeviceBatch:
 
     def rebuild(self, lod_max=4, mode="graph"):
         """mode: "graph" (replay the tuned configuration's CUDA graph),
-        "direct" (the tuned configuration launched directly) or "plain"
-        (one launch per chunk)."""
-        flags = {"graph": VP_REBUILD_GRAPH, "direct": VP_REBUILD_PERSISTENT, "plain": VP_REBUILD_PLAIN}[mode]
+        "direct" (the tuned configuration launched directly), "plain" (one
+        launch per chunk) or "concurrent" (one launch per chunk over 16
+        streams)."""
+        flags = {"graph": VP_REBUILD_GRAPH, "direct": VP_REBUILD_PERSISTENT, "plain": VP_REBUILD_PLAIN,
+                 "concurrent": VP_REBUILD_CONCURRENT}[mode]
         check(self.lib.vp_batch_rebuild(self.h, lod_max, flags), "vp_batch_rebuild")
 
     def finish(self):
