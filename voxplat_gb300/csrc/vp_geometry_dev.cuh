@@ -978,7 +978,8 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
 	uint32_t *ibo = (uint32_t *)aibo.base + s_base[1] * 4u;
 	const SmallAcc<RB> acc{S, stream, m};
 	/* pass 2: warps take the non-empty 32-row groups from a shared counter;
-	 * one face per lane per step, a second one when more than 32 remain */
+	 * one face per lane per step (a second face per step, with both
+	 * searches first, measured slower) */
 	for (;;) {
 		uint32_t t = 0;
 		if (lane == 0) t = atomicAdd(&s_next, 1u);
@@ -993,24 +994,16 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
 		const uint32_t excl = inc - c;
 		const uint32_t T = __shfl_sync(kFull, inc, 31);
 		const uint32_t base = m.grp[g];
-		for (uint32_t k = 0; k < T; k += 64) {
-			const bool two = k + 32 < T;
-			const uint32_t j0 = k + lane, j1 = k + 32 + lane;
-			const int s0 = search_lane(excl, j0), s1 = two ? search_lane(excl, j1) : 0;
-			const uint32_t e0 = __shfl_sync(kFull, excl, s0), e1 = __shfl_sync(kFull, excl, s1);
+		for (uint32_t k = 0; k < T; k += 32) {
+			const uint32_t j0 = k + lane;
+			const int s0 = search_lane(excl, j0);
+			const uint32_t e0 = __shfl_sync(kFull, excl, s0);
 			const uint64_t ax = shfl64(fx, s0), ay = shfl64(fy, s0), az = shfl64(fz, s0);
-			const uint64_t bx = shfl64(fx, s1), by = shfl64(fy, s1), bz = shfl64(fz, s1);
 			if (j0 < T) {
 				int x, i;
 				select_face<RB>(ax, ay, az, j0 - e0, x, i);
 				const int rr = (int)g * 32 + s0;
 				emit_face<RB>(acc, S, cv, x, rr & (R - 1), rr >> RB, i, base + j0, vbo, ibo);
-			}
-			if (two && j1 < T) {
-				int x, i;
-				select_face<RB>(bx, by, bz, j1 - e1, x, i);
-				const int rr = (int)g * 32 + s1;
-				emit_face<RB>(acc, S, cv, x, rr & (R - 1), rr >> RB, i, base + j1, vbo, ibo);
 			}
 		}
 	}
@@ -1101,27 +1094,38 @@ __device__ __forceinline__ void build_level(const Smem &m)
 	constexpr int R = Geo<RB>::R;
 	constexpr uint32_t n = (uint32_t)(R >> L) + 1u, np = (uint32_t)(R >> (L - 1)) + 1u;
 	uint64_t *dst = m.lv + c_lv.off[RB][L];
-	for (uint32_t i = threadIdx.x; i < n * n; i += blockDim.x) {
-		const uint32_t z = i / n, y = i - z * n;
-		uint64_t acc = 0;
-		uint32_t accx = 0;
+	const uint32_t lane = threadIdx.x & 31u;
+	/* warp-aligned: the 32 rows a warp writes are one emission group, whose
+	 * item count it records on the way (no separate count pass) */
+	for (uint32_t base = threadIdx.x & ~31u; base < n * n; base += blockDim.x) {
+		const uint32_t i = base + lane;
+		uint64_t row = 0;
+		if (i < n * n) {
+			const uint32_t z = i / n, y = i - z * n;
+			uint64_t acc = 0;
+			uint32_t accx = 0;
 #pragma unroll
-		for (uint32_t dz = 0; dz < 2; dz++)
+			for (uint32_t dz = 0; dz < 2; dz++)
 #pragma unroll
-			for (uint32_t dy = 0; dy < 2; dy++) {
-				const uint32_t yy = 2 * y + dy, zz = 2 * z + dz;
-				if (yy >= np || zz >= np) continue;
-				uint32_t xr;
-				acc |= level_row<RB>(m, L - 1, (int)yy, (int)zz, xr);
-				accx |= xr;
-			}
-		uint64_t row = compress_pairs(acc);
-		if (L == 1) row |= (uint64_t)accx << (R / 2);
-		dst[i] = row;
+				for (uint32_t dy = 0; dy < 2; dy++) {
+					const uint32_t yy = 2 * y + dy, zz = 2 * z + dz;
+					if (yy >= np || zz >= np) continue;
+					uint32_t xr;
+					acc |= level_row<RB>(m, L - 1, (int)yy, (int)zz, xr);
+					accx |= xr;
+				}
+			row = compress_pairs(acc);
+			if (L == 1) row |= (uint64_t)accx << (R / 2);
+			dst[i] = row;
+		}
+		const uint32_t c = __reduce_add_sync(kFull, (uint32_t)__popcll(row));
+		if (lane == 0) m.grp[c_lv.gstart[RB][L] + base / 32u] = c;
 	}
 }
 
-/* Cells of 32-row group g of level L (all lanes call; every lane gets it). */
+/* Cells of 32-row group g of level L (all lanes call; every lane gets it).
+ * Used for level 0, whose rows come from several sources; build_level
+ * counts the groups of the levels above as it writes their rows. */
 template <int RB, int L>
 __device__ __forceinline__ uint32_t count_group(const Smem &m, int g)
 {
@@ -1138,9 +1142,9 @@ __device__ __forceinline__ uint32_t count_group(const Smem &m, int g)
 }
 
 /* Pass 2 of one non-empty 32-row group of level L: lane s holds row s and
- * its exclusive item offset; items go one per lane per step, a second one
- * when more than 32 remain (both searches first, so their shuffle chains
- * overlap). Specialised per level, so the row division, the walk down and
+ * its exclusive item offset; items go one per lane per step (two per step,
+ * both searches first, measured 4 % slower: more registers live across the
+ * loads). Specialised per level, so the row division, the walk down and
  * the shifts are compile-time. */
 template <int RB, int L>
 __device__ __forceinline__ void splat_group(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m,
@@ -1162,25 +1166,16 @@ __device__ __forceinline__ void splat_group(const SetDesc &S, const uint32_t *__
 	const uint32_t excl = inc - c;
 	const uint32_t T = __shfl_sync(kFull, inc, 31);
 	const uint32_t base = m.grp[g];
-	for (uint32_t k = 0; k < T; k += 64) {
-		const bool two = k + 32 < T;
-		const uint32_t j0 = k + lane, j1 = k + 32 + lane;
+	for (uint32_t k = 0; k < T; k += 32) {
+		const uint32_t j0 = k + lane;
 		const int s0 = search_lane(excl, j0);
-		const int s1 = two ? search_lane(excl, j1) : 0;
 		const uint32_t e0 = __shfl_sync(kFull, excl, s0), q0 = __shfl_sync(kFull, yz, s0);
-		const uint32_t e1 = __shfl_sync(kFull, excl, s1), q1 = __shfl_sync(kFull, yz, s1);
-		const uint64_t w0 = shfl64(row, s0), w1 = shfl64(row, s1);
+		const uint64_t w0 = shfl64(row, s0);
 		if (j0 < T) {
 			const int kk = (int)(j0 - e0);
 			const int x = kk < __popcll(w0) ? select_bit(w0, kk) : R;
 			emit_splat<RB, L>(S, stream, m, cv, x, (int)(q0 & 0xFFFFu), (int)(q0 >> 16),
 					  dst + (size_t)(base + j0) * 4, sh_in);
-		}
-		if (two && j1 < T) {
-			const int kk = (int)(j1 - e1);
-			const int x = kk < __popcll(w1) ? select_bit(w1, kk) : R;
-			emit_splat<RB, L>(S, stream, m, cv, x, (int)(q1 & 0xFFFFu), (int)(q1 >> 16),
-					  dst + (size_t)(base + j1) * 4, sh_in);
 		}
 	}
 }
@@ -1207,20 +1202,11 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 		}
 		__syncthreads();
 	}
-	/* pass 1: splats per 32-row group, levels in order */
+	/* pass 1: splats per 32-row group; the level rows' groups were counted
+	 * as they were built, level 0's are counted here */
 	const int ngroups = gstart[lod_max + 1];
-	for (int g = warp; g < ngroups; g += nw) {
-		uint32_t c;
-		switch (group_level<RB>(g)) {
-		case 0: c = count_group<RB, 0>(m, g); break;
-		case 1: c = count_group<RB, 1>(m, g); break;
-		case 2: c = count_group<RB, 2>(m, g); break;
-		case 3: c = count_group<RB, 3>(m, g); break;
-		case 4: c = count_group<RB, 4>(m, g); break;
-		case 5: c = count_group<RB, 5>(m, g); break;
-		case 6: c = count_group<RB, 6>(m, g); break;
-		default: c = count_group<RB, 7>(m, g); break;
-		}
+	for (int g = warp; g < gstart[1]; g += nw) {
+		const uint32_t c = count_group<RB, 0>(m, g);
 		if (lane == 0) m.grp[g] = c;
 	}
 	__syncthreads();
