@@ -75,15 +75,70 @@ def workload_config(world, modes):
     }
 
 
-class ClockSampler:
-    """nvidia-smi clocks sampled during the timed region."""
+_REASON_BITS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+                0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
 
-    def __init__(self, index=0):
-        self.index = index
+
+class _Nvml:
+    """Read-only NVML queries through ctypes (SM clock, its maximum, power,
+    the active clock-event reasons). Nothing here sets anything."""
+
+    def __init__(self, index, pci=None):
+        import ctypes
+        self.c = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        ok = False
+        if pci:
+            for bus in ("0000" + pci, pci):
+                if self.lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(self.h)) == 0:
+                    ok = True
+                    break
+        if not ok and self.lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(self.h)) != 0:
+            raise RuntimeError("no NVML handle")
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.max_sm = self._uint(self.lib.nvmlDeviceGetMaxClockInfo, 1)
+
+    def _uint(self, fn, *args):
+        v = self.c.c_uint()
+        if fn(self.h, *args, self.c.byref(v)) != 0:
+            return None
+        return v.value
+
+    def sample(self):
+        r = self.c.c_ulonglong()
+        rs = r.value if self.reasons_fn(self.h, self.c.byref(r)) == 0 else 0
+        return self._uint(self.lib.nvmlDeviceGetClockInfo, 1), self._uint(self.lib.nvmlDeviceGetPowerUsage), rs
+
+    def close(self):
+        self.lib.nvmlShutdown()
+
+
+class ClockSampler:
+    """SM clocks and clock-event reasons sampled during the timed region:
+    NVML every 2 ms from a thread (the timed regions last tens of ms), or
+    nvidia-smi every 100 ms where NVML cannot be loaded."""
+
+    def __init__(self, index=0, pci=None, period_s=0.002):
+        self.index, self.pci, self.period = index, pci, period_s
         self.proc = None
+        self.nvml = None
         self.lines = []
+        self.samples = []
+        self.stop = threading.Event()
 
     def __enter__(self):
+        try:
+            self.nvml = _Nvml(self.index, self.pci)
+            self.samples.append(self.nvml.sample())
+            self.t = threading.Thread(target=self._poll, daemon=True)
+            self.t.start()
+            return self
+        except Exception:
+            self.nvml = None
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
@@ -97,11 +152,20 @@ class ClockSampler:
             self.proc = None
         return self
 
+    def _poll(self):
+        while not self.stop.wait(self.period):
+            self.samples.append(self.nvml.sample())
+
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        if self.nvml:
+            self.stop.set()
+            self.t.join(timeout=5)
+            self.samples.append(self.nvml.sample())
+            self.nvml.close()
         if self.proc:
             self.proc.terminate()
             try:
@@ -110,22 +174,38 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        sm, mx, reasons = [], 0.0, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            f = [x.strip() for x in ln.split(",")]
-            if len(f) < 8:
-                continue
-            try:
-                sm.append(float(f[1]))
-                mx = max(mx, float(f[2]))
-            except ValueError:
-                continue
-            for k, nm in enumerate(names):
-                if f[4 + k].lower().startswith("active"):
-                    reasons.add(nm)
+        sm, mx, reasons, pw = [], 0.0, set(), []
+        if self.nvml:
+            for clk, mw, rs in self.samples:
+                if clk is None:
+                    continue
+                sm.append(float(clk))
+                if mw is not None:
+                    pw.append(mw / 1e3)
+                for bit, nm in _REASON_BITS.items():
+                    if rs & bit:
+                        reasons.add(nm)
+            mx = float(self.nvml.max_sm or 0)
+            src = "nvml, every %g ms" % (self.period * 1e3)
+        else:
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for ln in self.lines:
+                f = [x.strip() for x in ln.split(",")]
+                if len(f) < 8:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx = max(mx, float(f[2]))
+                    pw.append(float(f[3]))
+                except ValueError:
+                    continue
+                for k, nm in enumerate(names):
+                    if f[4 + k].lower().startswith("active"):
+                        reasons.add(nm)
+            src = "nvidia-smi, every 100 ms"
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "sm_min_mhz": min(sm) if sm else None, "power_w": round(float(np.median(pw)), 1) if pw else None,
+                "reasons": sorted(reasons), "samples": len(sm), "source": src}
 
 
 def bind_near_gpu(dev):
@@ -263,7 +343,7 @@ def run_ours(args):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(dev) as clk:
+    with ClockSampler(dev, host_binding.get("pci")) as clk:
         for k in range(args.steps):
             with torch.cuda.stream(stream):
                 flush.zero_()
