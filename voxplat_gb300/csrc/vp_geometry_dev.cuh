@@ -672,6 +672,28 @@ __device__ __forceinline__ uint32_t mask_colour(const SetDesc &S, const uint32_t
 	return S.shell_col[(size_t)nc * G::shell_cols + (size_t)a * RR + idx];
 }
 
+/* mask_colour with the colour in the top byte of the word returned, so a
+ * stream word can be consumed (>> 24) after the next step's loads issue. */
+template <int RB>
+__device__ __forceinline__ uint32_t mask_colour_word(const SetDesc &S, const uint32_t *__restrict__ s, const Smem &m,
+						     int x, int y, int z)
+{
+	using G = Geo<RB>;
+	constexpr int R = G::R, RR = G::RR;
+	int a = -1, idx = 0;
+	if (x == R) { a = 0; idx = (z << RB) | y; }
+	else if (y == R) { a = 1; idx = (z << RB) | x; }
+	else if (z == R) { a = 2; idx = (y << RB) | x; }
+	if (a < 0) {
+		const int row = (z << RB) | y;
+		const uint64_t bits = m.rs[row] & (~0ull >> (63 - x));
+		return __ldg(s + (m.rank[row] + __popcll(bits) - 1u));
+	}
+	const int32_t nc = m.nbr[nbr_slot(a == 0, a == 1, a == 2)];
+	if (nc < 0) return 0u;
+	return (uint32_t)S.shell_col[(size_t)nc * G::shell_cols + (size_t)a * RR + idx] << 24;
+}
+
 static __device__ __forceinline__ void store_splat(int16_t *dst, uint32_t x, uint32_t y, uint32_t z, uint32_t w)
 {
 	uint2 v;
@@ -1061,6 +1083,66 @@ __device__ __forceinline__ void emit_splat(const SetDesc &S, const uint32_t *__r
 	store_splat(dst, wx, wy, wz, colour | (shadow << 6));
 }
 
+/* emit_splat in two halves for the pipelined level-0 loop: splat_issue
+ * walks down, issues the colour and shadow loads and stores the splat's x
+ * and y; splat_finish, one step later, stores z and colour | shadow << 6
+ * from the loaded values. */
+struct SplatPend {
+	uint32_t vz, c, a, b, lim;
+};
+
+template <int RB, int L>
+__device__ __forceinline__ void splat_issue(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m,
+					    const uint32_t cv[3], int x, int y, int z, bool sh_in, int16_t *dst, SplatPend &p)
+{
+	constexpr int R = Geo<RB>::R;
+	int cx = x, cy = y, cz = z;
+#pragma unroll
+	for (int lc = L - 1; lc >= 0; lc--) {
+		const int np = (R >> lc) + 1;
+		const int X = 2 * cx;
+		uint32_t pat = 0;
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			const int Y = 2 * cy + (q & 1), Z = 2 * cz + (q >> 1);
+			if (Y < np && Z < np) {
+				uint32_t xr;
+				const uint64_t row = level_row<RB>(m, lc, Y, Z, xr);
+				const uint32_t b2 = (lc == 0 && X == R) ? xr : (uint32_t)((row >> X) & 3ull);
+				pat |= b2 << (2 * q);
+			}
+		}
+		const int best = pat ? 31 - __clz(pat) : 0;
+		cx = X + (best & 1);
+		cy = 2 * cy + ((best >> 1) & 1);
+		cz = 2 * cz + (best >> 2);
+	}
+	p.c = mask_colour_word<RB>(S, stream, m, cx, cy, cz);
+	constexpr uint32_t sh = L ? (1u << L) : 0u;
+	const uint32_t wx = (cv[0] << RB) + ((uint32_t)x << L);
+	const uint32_t wy = (cv[1] << RB) + ((uint32_t)y << L);
+	const uint32_t wz = (cv[2] << RB) + ((uint32_t)z << L);
+	*(uint32_t *)dst = (wx & 0xFFFFu) | ((wy & 0xFFFFu) << 16); /* x, y now; z and w in splat_finish */
+	p.vz = wz & 0xFFFFu;
+	p.lim = wy + sh + 1u; /* 0 after a wrap: nothing is < 0, the splat is shadowed */
+	if (sh_in) {
+		const uint16_t *q = S.shadow + (((uint64_t)((wx + sh) + (wy + sh)) + (uint64_t)S.shadow_w * (wz + sh)) -
+						S.shadow_base);
+		p.a = __ldg(q);
+		p.b = __ldg(q + 1);
+	} else {
+		const uint32_t idx = ((wx + sh) + (wy + sh)) + S.shadow_w * (wz + sh);
+		p.a = shadow_at(S, idx);
+		p.b = shadow_at(S, idx + 1u);
+	}
+}
+
+__device__ __forceinline__ void splat_finish(int16_t *dst, const SplatPend &p)
+{
+	const uint32_t shadow = !((p.a < p.lim) & (p.b < p.lim));
+	((uint32_t *)dst)[1] = p.vz | (((p.c >> 24) | (shadow << 6)) << 16);
+}
+
 /* Whether every shadow sample of a chunk's splats (world coordinates up to
  * its far corner plus 2^lod_max, and the entry after) falls inside the map
  * and needs no uint32 wrap. */
@@ -1145,7 +1227,10 @@ __device__ __forceinline__ uint32_t count_group(const Smem &m, int g)
  * its exclusive item offset; items go one per lane per step (two per step,
  * both searches first, measured 4 % slower: more registers live across the
  * loads). Specialised per level, so the row division, the walk down and
- * the shifts are compile-time. */
+ * the shifts are compile-time. Level 0 (three quarters of the splats) is
+ * software-pipelined: a step's colour and shadow loads are issued, and
+ * consumed one step later, after the next step's search and select. The
+ * levels above keep the plain loop: their walk down needs the registers. */
 template <int RB, int L>
 __device__ __forceinline__ void splat_group(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m,
 					    const uint32_t cv[3], int g, int16_t *dst, bool sh_in)
@@ -1166,18 +1251,44 @@ __device__ __forceinline__ void splat_group(const SetDesc &S, const uint32_t *__
 	const uint32_t excl = inc - c;
 	const uint32_t T = __shfl_sync(kFull, inc, 31);
 	const uint32_t base = m.grp[g];
+	if (L != 0) {
+		for (uint32_t k = 0; k < T; k += 32) {
+			const uint32_t j0 = k + lane;
+			const int s0 = search_lane(excl, j0);
+			const uint32_t e0 = __shfl_sync(kFull, excl, s0), q0 = __shfl_sync(kFull, yz, s0);
+			const uint64_t w0 = shfl64(row, s0);
+			if (j0 < T) {
+				const int kk = (int)(j0 - e0);
+				const int x = kk < __popcll(w0) ? select_bit(w0, kk) : R;
+				emit_splat<RB, L>(S, stream, m, cv, x, (int)(q0 & 0xFFFFu), (int)(q0 >> 16),
+						  dst + (size_t)(base + j0) * 4, sh_in);
+			}
+		}
+		return;
+	}
+	SplatPend pend;
+	bool pv = false;
+	uint32_t pj = 0;
 	for (uint32_t k = 0; k < T; k += 32) {
 		const uint32_t j0 = k + lane;
 		const int s0 = search_lane(excl, j0);
 		const uint32_t e0 = __shfl_sync(kFull, excl, s0), q0 = __shfl_sync(kFull, yz, s0);
 		const uint64_t w0 = shfl64(row, s0);
-		if (j0 < T) {
+		const bool v = j0 < T;
+		int x = 0;
+		if (v) {
 			const int kk = (int)(j0 - e0);
-			const int x = kk < __popcll(w0) ? select_bit(w0, kk) : R;
-			emit_splat<RB, L>(S, stream, m, cv, x, (int)(q0 & 0xFFFFu), (int)(q0 >> 16),
-					  dst + (size_t)(base + j0) * 4, sh_in);
+			x = kk < __popcll(w0) ? select_bit(w0, kk) : R;
 		}
+		/* the previous step's loads had the search and select to land */
+		if (pv) splat_finish(dst + (size_t)(base + pj) * 4, pend);
+		if (v)
+			splat_issue<RB, L>(S, stream, m, cv, x, (int)(q0 & 0xFFFFu), (int)(q0 >> 16), sh_in,
+					   dst + (size_t)(base + j0) * 4, pend);
+		pv = v;
+		pj = j0;
 	}
+	if (pv) splat_finish(dst + (size_t)(base + pj) * 4, pend);
 }
 
 template <int RB>
