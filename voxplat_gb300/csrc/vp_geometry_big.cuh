@@ -455,17 +455,6 @@ __device__ __forceinline__ void level_row_big(const BigMem &m, int l, int y, int
 	a = m.lv[c_lv.off[7][l] + 65 * 65 + z * n + y];
 }
 
-/* x of the k-th cell of a level row (a, b, xr) */
-__device__ __forceinline__ int select_cell_big(uint64_t a, uint64_t b, int l, int k)
-{
-	const int ca = __popcll(a);
-	if (k < ca) return select_bit(a, k);
-	k -= ca;
-	const int cb = __popcll(b);
-	if (k < cb) return 64 + select_bit(b, k);
-	return Big::R >> l;
-}
-
 __device__ __forceinline__ uint32_t mask_colour_big(const SetDesc &S, const uint32_t *__restrict__ s, const BigMem &m,
 						   int x, int y, int z)
 {
@@ -480,13 +469,17 @@ __device__ __forceinline__ uint32_t mask_colour_big(const SetDesc &S, const uint
 	return S.shell_col[(size_t)nc * Big::shell_cols + (size_t)a * RR + idx];
 }
 
-/* One level-l splat, as emit_splat. */
+/* One level-L splat, as emit_splat: walk down (compile-time levels),
+ * colour, shadow (bounds-free when the chunk's sample window lies inside
+ * the map), store. */
+template <int L>
 __device__ __forceinline__ void emit_splat_big(const SetDesc &S, const uint32_t *__restrict__ stream, const BigMem &m,
-					       const uint32_t cv[3], int l, int x, int y, int z, int16_t *dst)
+					       const uint32_t cv[3], int x, int y, int z, int16_t *dst, bool sh_in)
 {
 	constexpr int R = Big::R;
 	int cx = x, cy = y, cz = z;
-	for (int lc = l - 1; lc >= 0; lc--) {
+#pragma unroll
+	for (int lc = L - 1; lc >= 0; lc--) {
 		const int np = (R >> lc) + 1;
 		const int X = 2 * cx;
 		const int xpos = lc <= 1 ? (R >> lc) : (1 << 30);
@@ -512,76 +505,155 @@ __device__ __forceinline__ void emit_splat_big(const SetDesc &S, const uint32_t 
 		cz = 2 * cz + (best >> 2);
 	}
 	const uint32_t colour = mask_colour_big(S, stream, m, cx, cy, cz);
-	const uint32_t sh = l ? (1u << l) : 0u;
-	const uint32_t wx = (cv[0] << 7) + ((uint32_t)x << l);
-	const uint32_t wy = (cv[1] << 7) + ((uint32_t)y << l);
-	const uint32_t wz = (cv[2] << 7) + ((uint32_t)z << l);
-	const uint32_t shadow = (uint32_t)shadow_sample(S, wx + sh, wy + sh, wz + sh);
+	constexpr uint32_t sh = L ? (1u << L) : 0u;
+	const uint32_t wx = (cv[0] << 7) + ((uint32_t)x << L);
+	const uint32_t wy = (cv[1] << 7) + ((uint32_t)y << L);
+	const uint32_t wz = (cv[2] << 7) + ((uint32_t)z << L);
+	uint32_t shadow;
+	if (sh_in) {
+		const uint32_t lim = wy + sh + 1u;
+		const uint16_t *p = S.shadow + (((uint64_t)((wx + sh) + (wy + sh)) + (uint64_t)S.shadow_w * (wz + sh)) -
+						S.shadow_base);
+		shadow = !((__ldg(p) < lim) & (__ldg(p + 1) < lim));
+	} else {
+		shadow = (uint32_t)shadow_sample(S, wx + sh, wy + sh, wz + sh);
+	}
 	store_splat(dst, wx, wy, wz, colour | (shadow << 6));
+}
+
+/* Level-L rows (L >= 1) of a 128^3 chunk, each 32-row group counted as a
+ * warp writes it (the warp's 32 rows are one emission group). */
+template <int L>
+__device__ __forceinline__ void build_level_big(const BigMem &m)
+{
+	constexpr uint32_t n = (uint32_t)big_n_at(L), np = (uint32_t)big_n_at(L - 1);
+	const uint32_t lane = threadIdx.x & 31u;
+	for (uint32_t base = threadIdx.x & ~31u; base < n * n; base += blockDim.x) {
+		const uint32_t i = base + lane;
+		uint32_t c = 0;
+		if (i < n * n) {
+			const uint32_t z = i / n, y = i - z * n;
+			uint64_t acc0 = 0, acc1 = 0;
+			uint32_t accx = 0;
+#pragma unroll
+			for (uint32_t dz = 0; dz < 2; dz++)
+#pragma unroll
+				for (uint32_t dy = 0; dy < 2; dy++) {
+					const uint32_t yy = 2 * y + dy, zz = 2 * z + dz;
+					if (yy >= np || zz >= np) continue;
+					uint64_t a, b;
+					uint32_t xr;
+					level_row_big(m, L - 1, (int)yy, (int)zz, a, b, xr);
+					acc0 |= a;
+					acc1 |= b;
+					accx |= xr;
+				}
+			if (L == 1) {
+				const uint64_t row = compress_pairs(acc0) | (compress_pairs(acc1) << 32);
+				m.lv[2 * (size_t)i] = row;
+				m.lv[2 * (size_t)i + 1] = accx;
+				c = (uint32_t)__popcll(row) + accx;
+			} else if (L == 2) {
+				const uint64_t row = compress_pairs(acc0) | ((uint64_t)accx << 32);
+				m.lv[big_lv_off(2) + i] = row;
+				c = (uint32_t)__popcll(row);
+			} else {
+				const uint64_t row = compress_pairs(acc0);
+				m.lv[c_lv.off[7][L] + 65 * 65 + i] = row;
+				c = (uint32_t)__popcll(row);
+			}
+		}
+		c = __reduce_add_sync(kFull, c);
+		if (lane == 0) m.grp[c_lv.gstart[7][L] + base / 32u] = c;
+	}
+}
+
+/* Pass 2 of one non-empty 32-row group of level L, as splat_group. */
+template <int L>
+__device__ __forceinline__ void splat_group_big(const SetDesc &S, const uint32_t *__restrict__ stream, const BigMem &m,
+						const uint32_t cv[3], int g, int16_t *dst, bool sh_in)
+{
+	constexpr int R = Big::R;
+	constexpr uint32_t n = (uint32_t)big_n_at(L);
+	const int lane = threadIdx.x & 31;
+	const uint32_t r = (uint32_t)(g - c_lv.gstart[7][L]) * 32u + (uint32_t)lane;
+	uint64_t a = 0, b = 0;
+	uint32_t xr = 0, yz = 0;
+	if (r < n * n) {
+		const uint32_t z = r / n, y = r - z * n;
+		level_row_big(m, L, (int)y, (int)z, a, b, xr);
+		yz = y | (z << 16);
+	}
+	const uint32_t c = (uint32_t)__popcll(a) + (L == 0 ? (uint32_t)__popcll(b) : 0u) + xr;
+	const uint32_t inc = warp_incl_add(c);
+	const uint32_t excl = inc - c;
+	const uint32_t T = __shfl_sync(kFull, inc, 31);
+	const uint32_t base = m.grp[g];
+	for (uint32_t k = 0; k < T; k += 32) {
+		const uint32_t j0 = k + (uint32_t)lane;
+		const int s0 = search_lane(excl, j0);
+		const uint32_t e0 = __shfl_sync(kFull, excl, s0), q0 = __shfl_sync(kFull, yz, s0);
+		const uint64_t wa = shfl64(a, s0);
+		const uint64_t wb = L == 0 ? shfl64(b, s0) : 0ull;
+		if (j0 < T) {
+			int kk = (int)(j0 - e0);
+			int x;
+			const int ca = __popcll(wa);
+			if (kk < ca) {
+				x = select_bit(wa, kk);
+			} else if (L == 0) {
+				kk -= ca;
+				x = kk < __popcll(wb) ? 64 + select_bit(wb, kk) : R;
+			} else {
+				x = R >> L; /* level 1: the x = 64 cell (levels >= 2 hold it in a) */
+			}
+			emit_splat_big<L>(S, stream, m, cv, x, (int)(q0 & 0xFFFFu), (int)(q0 >> 16),
+					  dst + (size_t)(base + j0) * 4, sh_in);
+		}
+	}
 }
 
 static __device__ void splat_chunk_big(const SetDesc &S, const uint32_t *__restrict__ stream, const BigMem &m,
 				const uint32_t cv[3], int lod_max, ChunkOut *out, const Arena &asvl)
 {
-	constexpr int R = Big::R;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 	__shared__ unsigned long long s_base;
 	__shared__ uint32_t s_ok, s_next;
+	__shared__ uint16_t s_glist[big_max_groups()];
 	const int *gstart = c_lv.gstart[7];
 	splat_prepare_big(m);
-	/* level rows: pairwise OR of the child rows, compacted along x */
+	/* level rows: pairwise OR of the child rows, compacted along x; their
+	 * groups are counted as they are written */
 	for (int l = 1; l <= lod_max; l++) {
-		const int n = (R >> l) + 1, np = (R >> (l - 1)) + 1;
-		const uint32_t mg = c_lv.magic[7][l];
-		for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
-			int y, z;
-			row_yz((uint32_t)i, (uint32_t)n, mg, y, z);
-			uint64_t acc0 = 0, acc1 = 0;
-			uint32_t accx = 0;
-			for (int dz = 0; dz < 2; dz++)
-				for (int dy = 0; dy < 2; dy++) {
-					const int yy = 2 * y + dy, zz = 2 * z + dz;
-					if (yy >= np || zz >= np) continue;
-					uint64_t a, b;
-					uint32_t xr;
-					level_row_big(m, l - 1, yy, zz, a, b, xr);
-					acc0 |= a;
-					acc1 |= b;
-					accx |= xr;
-				}
-			if (l == 1) {
-				m.lv[2 * (size_t)i] = compress_pairs(acc0) | (compress_pairs(acc1) << 32);
-				m.lv[2 * (size_t)i + 1] = accx;
-			} else if (l == 2) {
-				m.lv[big_lv_off(2) + i] = compress_pairs(acc0) | ((uint64_t)accx << 32);
-			} else {
-				m.lv[c_lv.off[7][l] + 65 * 65 + i] = compress_pairs(acc0);
-			}
+		switch (l) {
+		case 1: build_level_big<1>(m); break;
+		case 2: build_level_big<2>(m); break;
+		case 3: build_level_big<3>(m); break;
+		case 4: build_level_big<4>(m); break;
+		case 5: build_level_big<5>(m); break;
+		case 6: build_level_big<6>(m); break;
+		default: build_level_big<7>(m); break;
 		}
 		__syncthreads();
 	}
-	/* pass 1: cells per 32-row group, levels in order */
+	/* pass 1: level 0's groups */
 	const int ngroups = gstart[lod_max + 1];
-	for (int g = warp; g < ngroups; g += nw) {
-		int l = 0;
-		while (g >= gstart[l + 1]) l++;
-		const int n = (R >> l) + 1;
-		const int r = (g - gstart[l]) * 32 + lane;
+	for (int g = warp; g < gstart[1]; g += nw) {
+		const int r = g * 32 + lane;
 		uint32_t c = 0;
-		if (r < n * n) {
-			int y, z;
-			row_yz((uint32_t)r, (uint32_t)n, c_lv.magic[7][l], y, z);
+		if (r < 129 * 129) {
+			const int z = r / 129, y = r - z * 129;
 			uint64_t a, b;
 			uint32_t xr;
-			level_row_big(m, l, y, z, a, b, xr);
-			c = __popcll(a) + __popcll(b) + xr;
+			e0_row_big(m, y, z, a, b, xr);
+			c = (uint32_t)(__popcll(a) + __popcll(b)) + xr;
 		}
-#pragma unroll
-		for (int d = 16; d; d >>= 1) c += __shfl_xor_sync(kFull, c, d);
+		c = __reduce_add_sync(kFull, c);
 		if (lane == 0) m.grp[g] = c;
 	}
 	__syncthreads();
-	const uint32_t total = scan_groups(m.grp, ngroups, m.tmp);
+	const uint32_t total = scan_groups(m.grp, ngroups, m.tmp, s_glist);
+	const uint32_t listed = m.tmp[1];
 	if (threadIdx.x == 0) {
 		const uint64_t units = ((uint64_t)total + 1u) / 2u; /* 8 B per splat */
 		unsigned long long b = units ? atomicAdd(asvl.cursor, (unsigned long long)units) : 0ull;
@@ -607,39 +679,23 @@ static __device__ void splat_chunk_big(const SetDesc &S, const uint32_t *__restr
 	__syncthreads();
 	if (!s_ok) return;
 	int16_t *dst = (int16_t *)asvl.base + s_base * 8u;
-	/* pass 2: warps take groups from a shared counter */
+	const bool sh_in = shadow_window_inside<7>(S, cv, lod_max);
+	/* pass 2: warps take the non-empty groups from a shared counter */
 	for (;;) {
-		uint32_t g = 0;
-		if (lane == 0) g = atomicAdd(&s_next, 1u);
-		g = __shfl_sync(kFull, g, 0);
-		if (g >= (uint32_t)ngroups) break;
-		int l = 0;
-		while ((int)g >= gstart[l + 1]) l++;
-		const int n = (R >> l) + 1;
-		const int r = ((int)g - gstart[l]) * 32 + lane;
-		uint64_t a = 0, b = 0;
-		uint32_t xr = 0, yz = 0;
-		if (r < n * n) {
-			int y, z;
-			row_yz((uint32_t)r, (uint32_t)n, c_lv.magic[7][l], y, z);
-			level_row_big(m, l, y, z, a, b, xr);
-			yz = (uint32_t)y | ((uint32_t)z << 16);
-		}
-		const uint32_t c = __popcll(a) + __popcll(b) + xr;
-		const uint32_t inc = warp_incl_add(c);
-		const uint32_t excl = inc - c;
-		const uint32_t T = __shfl_sync(kFull, inc, 31);
-		const uint32_t base = m.grp[g];
-		for (uint32_t k = 0; k < T; k += 32) {
-			const uint32_t j = k + lane;
-			const int s = search_lane(excl, j);
-			const uint32_t e = __shfl_sync(kFull, excl, s), q = __shfl_sync(kFull, yz, s);
-			const uint64_t wa = shfl64(a, s), wb = shfl64(b, s);
-			if (j < T) {
-				const int x = select_cell_big(wa, wb, l, (int)(j - e));
-				emit_splat_big(S, stream, m, cv, l, x, (int)(q & 0xFFFFu), (int)(q >> 16),
-					       dst + (size_t)(base + j) * 4);
-			}
+		uint32_t k = 0;
+		if (lane == 0) k = atomicAdd(&s_next, 1u);
+		k = __shfl_sync(kFull, k, 0);
+		if (k >= listed) break;
+		const int g = s_glist[k];
+		switch (group_level<7>(g)) {
+		case 0: splat_group_big<0>(S, stream, m, cv, g, dst, sh_in); break;
+		case 1: splat_group_big<1>(S, stream, m, cv, g, dst, sh_in); break;
+		case 2: splat_group_big<2>(S, stream, m, cv, g, dst, sh_in); break;
+		case 3: splat_group_big<3>(S, stream, m, cv, g, dst, sh_in); break;
+		case 4: splat_group_big<4>(S, stream, m, cv, g, dst, sh_in); break;
+		case 5: splat_group_big<5>(S, stream, m, cv, g, dst, sh_in); break;
+		case 6: splat_group_big<6>(S, stream, m, cv, g, dst, sh_in); break;
+		default: splat_group_big<7>(S, stream, m, cv, g, dst, sh_in); break;
 		}
 	}
 }
