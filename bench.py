@@ -588,17 +588,26 @@ def edit_trace(seed, n, rate, extent_xz, band=(8, 56), rmax=32):
     return gpu.make_edits(rows, arrival)
 
 
-def uneven_batch(ctx, n=4096, seed=3, steps=5):
+def uneven_batch(ctx, n=4096, seed=3, steps=5, root=None):
     """4096 standalone chunks, roots 32/64/128 in ratio 1:6:1, occupancy
     log-uniform 0.1%..100% (noise blobs + uniform random voxels), colours
     1..255; splats LOD 0..4. Batched = the autotuned configuration replayed
-    as a CUDA graph (one persistent launch); plain = one launch per chunk."""
+    as a CUDA graph (one persistent launch); plain = one launch per chunk.
+    With `root` (5, 6 or 7), the first n chunks of the same sequence with
+    that root only (a smaller case of one kernel, for profiling)."""
     from concurrent.futures import ThreadPoolExecutor
     from voxplat_gb300 import gpu
     from voxplat_gb300 import worldgen as wg
     t0 = time.perf_counter()
+    ks = list(range(n))
+    if root is not None:
+        ks, k = [], 0
+        while len(ks) < n:
+            if wg.uneven_root_bitw(seed, k) == root:
+                ks.append(k)
+            k += 1
     with ThreadPoolExecutor(max(1, min(16, os.cpu_count() or 1))) as ex:
-        ws = list(ex.map(lambda k: wg.uneven_chunk(seed, k), range(n)))
+        ws = list(ex.map(lambda k: wg.uneven_chunk(seed, k), ks))
     gen_s = time.perf_counter() - t0
     b = gpu.DeviceBatch(ctx, ws)
     del ws
@@ -897,9 +906,17 @@ def main():
     ap.add_argument("--skip-edits", action="store_true", help="skip the edit-serving sub-benchmark")
     ap.add_argument("--skip-full-scale", action="store_true", help="skip the 524288-chunk full-scale rebuild")
     ap.add_argument("--skip-uneven", action="store_true", help="skip the mixed-root batch sub-benchmark")
+    ap.add_argument("--uneven-only", type=int, nargs=2, metavar=("ROOT_BITW", "N"),
+                    help="run only the mixed-root batch, restricted to its first N chunks of one root "
+                         "(a small case for profiling); prints that sub-benchmark's line")
     args = ap.parse_args()
     import __graft_entry__
     __graft_entry__.build()
+    if args.uneven_only:
+        from voxplat_gb300 import gpu
+        root, n = args.uneven_only
+        print(json.dumps(uneven_batch(gpu.Context(0), n=n, root=root)), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
