@@ -474,7 +474,8 @@ __device__ __forceinline__ uint32_t mask_colour_big(const SetDesc &S, const uint
  * the map), store. */
 template <int L>
 __device__ __forceinline__ void emit_splat_big(const SetDesc &S, const uint32_t *__restrict__ stream, const BigMem &m,
-					       const uint32_t cv[3], int x, int y, int z, int16_t *dst, bool sh_in)
+					       const uint32_t cv[3], int x, int y, int z, int16_t *dst, bool sh_in,
+					       int colour_in = -1)
 {
 	constexpr int R = Big::R;
 	int cx = x, cy = y, cz = z;
@@ -504,7 +505,7 @@ __device__ __forceinline__ void emit_splat_big(const SetDesc &S, const uint32_t 
 		cy = 2 * cy + ((best >> 1) & 1);
 		cz = 2 * cz + (best >> 2);
 	}
-	const uint32_t colour = mask_colour_big(S, stream, m, cx, cy, cz);
+	const uint32_t colour = (L == 0 && colour_in >= 0) ? (uint32_t)colour_in : mask_colour_big(S, stream, m, cx, cy, cz);
 	constexpr uint32_t sh = L ? (1u << L) : 0u;
 	const uint32_t wx = (cv[0] << 7) + ((uint32_t)x << L);
 	const uint32_t wy = (cv[1] << 7) + ((uint32_t)y << L);
@@ -579,10 +580,20 @@ __device__ __forceinline__ void splat_group_big(const SetDesc &S, const uint32_t
 	const uint32_t r = (uint32_t)(g - c_lv.gstart[7][L]) * 32u + (uint32_t)lane;
 	uint64_t a = 0, b = 0;
 	uint32_t xr = 0, yz = 0;
+	/* level 0: the row's run starts and rank, read once per row (global
+	 * scratch) and handed to the row's items by shuffles */
+	uint64_t rsa = 0, rsb = 0;
+	uint32_t rk = 0;
 	if (r < n * n) {
 		const uint32_t z = r / n, y = r - z * n;
 		level_row_big(m, L, (int)y, (int)z, a, b, xr);
 		yz = y | (z << 16);
+		if (L == 0 && y < (uint32_t)R && z < (uint32_t)R) {
+			const uint32_t row = (z << 7) | y;
+			rsa = m.rs[2 * row];
+			rsb = m.rs[2 * row + 1];
+			rk = m.rank[row];
+		}
 	}
 	const uint32_t c = (uint32_t)__popcll(a) + (L == 0 ? (uint32_t)__popcll(b) : 0u) + xr;
 	const uint32_t inc = warp_incl_add(c);
@@ -595,6 +606,8 @@ __device__ __forceinline__ void splat_group_big(const SetDesc &S, const uint32_t
 		const uint32_t e0 = __shfl_sync(kFull, excl, s0), q0 = __shfl_sync(kFull, yz, s0);
 		const uint64_t wa = shfl64(a, s0);
 		const uint64_t wb = L == 0 ? shfl64(b, s0) : 0ull;
+		const uint64_t ra = L == 0 ? shfl64(rsa, s0) : 0ull, rb = L == 0 ? shfl64(rsb, s0) : 0ull;
+		const uint32_t rk0 = L == 0 ? __shfl_sync(kFull, rk, s0) : 0u;
 		if (j0 < T) {
 			int kk = (int)(j0 - e0);
 			int x;
@@ -607,8 +620,14 @@ __device__ __forceinline__ void splat_group_big(const SetDesc &S, const uint32_t
 			} else {
 				x = R >> L; /* level 1: the x = 64 cell (levels >= 2 hold it in a) */
 			}
-			emit_splat_big<L>(S, stream, m, cv, x, (int)(q0 & 0xFFFFu), (int)(q0 >> 16),
-					  dst + (size_t)(base + j0) * 4, sh_in);
+			const int y = (int)(q0 & 0xFFFFu), z = (int)(q0 >> 16);
+			int col = -1;
+			if (L == 0 && x < R && y < R && z < R) {
+				const uint32_t cnt = x < 64 ? (uint32_t)__popcll(ra & (~0ull >> (63 - x)))
+							    : (uint32_t)(__popcll(ra) + __popcll(rb & (~0ull >> (127 - x))));
+				col = (int)(__ldg(stream + (rk0 + cnt - 1u)) >> 24);
+			}
+			emit_splat_big<L>(S, stream, m, cv, x, y, z, dst + (size_t)(base + j0) * 4, sh_in, col);
 		}
 	}
 }
