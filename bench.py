@@ -767,23 +767,26 @@ def picking(dw, n=65536, seed=6):
             "hit_fraction": round(float((vox > 0).mean()), 3)}
 
 
-def full_scale(ctx, steps=3):
+def full_scale(ctx, steps=3, bits=(8, 8)):
     """16384x512x16384 world (256x8x256 = 524288 chunks of 64^3, 128 GiB of
     voxels), terrain + caves at 4x horizontal noise scale, generated and kept
     RLE-resident on the device; full rebuild with LOD 0..5, splats/meshes
-    and LOD/octree grouping."""
+    and LOD/octree grouping. `bits` (x and z chunk bit widths) give the
+    corner of the same world at a smaller size, for profiling."""
     import torch
     from voxplat_gb300 import gpu
     from voxplat_gb300 import worldgen as wg
+    bx, bz = bits
     t0 = time.perf_counter()
-    dw = gpu.DeviceWorld.generated(ctx, wg.TERRAIN_CAVES, 6, (8, 3, 8), seed=99, hshift=2)
+    dw = gpu.DeviceWorld.generated(ctx, wg.TERRAIN_CAVES, 6, (bx, 3, bz), seed=99, hshift=2)
     gen_s = time.perf_counter() - t0
     n = dw.nchunks
     c = np.arange(n)
-    xs = (c & 255) * 64 + 32
-    ys = ((c >> 8) & 7) * 64 + 32
-    zs = (c >> 11) * 64 + 32
-    modes = (np.sqrt((xs - 8192.0) ** 2 + (ys - 160.0) ** 2 + (zs - 8192.0) ** 2) < MESH_RADIUS).astype(np.uint8)
+    xs = (c & ((1 << bx) - 1)) * 64 + 32
+    ys = ((c >> bx) & 7) * 64 + 32
+    zs = (c >> (bx + 3)) * 64 + 32
+    cx, cz = (1 << bx) * 32.0, (1 << bz) * 32.0
+    modes = (np.sqrt((xs - cx) ** 2 + (ys - 160.0) ** 2 + (zs - cz) ** 2) < MESH_RADIUS).astype(np.uint8)
     dw.set_modes(modes)
     dw.rebuild(5, group=True)
     dw.finish()
@@ -831,8 +834,9 @@ def full_scale(ctx, steps=3):
     splats = int(res["svl_total"].astype(np.int64).sum()) // 4
     faces = int(res["ibo_items"].astype(np.int64).sum()) // 6
     out = {
-        "workload": "16384x512x16384 world (256x8x256 = 524288 chunks of 64^3), terrain+caves at 4x horizontal "
-                    "noise scale, RLE-resident; LOD 0..5, splats/meshes, LOD/octree grouping",
+        "workload": "%dx512x%d world (%dx8x%d = %d chunks of 64^3), terrain+caves at 4x horizontal "
+                    "noise scale, RLE-resident; LOD 0..5, splats/meshes, LOD/octree grouping"
+                    % (64 << bx, 64 << bz, 1 << bx, 1 << bz, n),
         "chunks": n,
         "ms_per_rebuild": round(ms, 3),
         "chunks_per_s": round(n / (ms / 1e3), 1),
@@ -909,6 +913,9 @@ def main():
     ap.add_argument("--uneven-only", type=int, nargs=2, metavar=("ROOT_BITW", "N"),
                     help="run only the mixed-root batch, restricted to its first N chunks of one root "
                          "(a small case for profiling); prints that sub-benchmark's line")
+    ap.add_argument("--full-scale-only", type=int, nargs=2, metavar=("BITS_X", "BITS_Z"),
+                    help="run only the full-scale rebuild, on the corner of its world 2^BITS_X x 8 x 2^BITS_Z "
+                         "chunks (8 8 is the full world); prints that sub-benchmark's line")
     args = ap.parse_args()
     import __graft_entry__
     __graft_entry__.build()
@@ -916,6 +923,13 @@ def main():
         from voxplat_gb300 import gpu
         root, n = args.uneven_only
         print(json.dumps(uneven_batch(gpu.Context(0), n=n, root=root)), flush=True)
+        return
+    if args.full_scale_only:
+        from voxplat_gb300 import gpu
+        fs = full_scale(gpu.Context(0), steps=2, bits=tuple(args.full_scale_only))
+        fs.pop("_dw").close()
+        fs.pop("_res")
+        print(json.dumps(fs), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -420,15 +420,25 @@ __global__ void __launch_bounds__(512, 2) k_shell(const SetDesc *__restrict__ se
 	}
 	/* low planes' colours: X0[z][y] = (0,y,z), Y0[z][x] = (x,0,z),
 	 * Z0[y][x] = (x,y,0) */
+	/* branch-free: the three lookups of two cells are in flight together
+	 * (an air cell reads a valid word and keeps 0) */
+#pragma unroll 2
 	for (int i = threadIdx.x; i < RR; i += blockDim.x) {
 		const int a = i & (R - 1), b = i >> RB;
-		uint32_t c0 = 0, c1 = 0, c2 = 0;
-		if ((m.occ[hidx<RB>(a, b)] & 1ull)) c0 = colour_at<RB>(stream, m, 0, a, b);
-		if ((m.occ[hidx<RB>(0, b)] >> a) & 1ull) c1 = colour_at<RB>(stream, m, a, 0, b);
-		if ((m.occ[hidx<RB>(b, 0)] >> a) & 1ull) c2 = colour_at<RB>(stream, m, a, b, 0);
-		cols[i] = (uint8_t)c0;
-		cols[RR + i] = (uint8_t)c1;
-		cols[2 * RR + i] = (uint8_t)c2;
+		const int r0 = (b << RB) | a, r1 = (b << RB);
+		const uint64_t o0 = m.occ[hidx<RB>(a, b)], o1 = m.occ[hidx<RB>(0, b)], o2 = m.occ[hidx<RB>(b, 0)];
+		const bool s0 = (o0 & 1ull) != 0, s1 = ((o1 >> a) & 1ull) != 0, s2 = ((o2 >> a) & 1ull) != 0;
+		/* (0, a, b): row (a, b), x = 0; (a, 0, b): row (0, b), x = a;
+		 * (a, b, 0): row (b, 0), x = a */
+		const int ra = r0, rb = r1, rc = b;
+		const uint32_t k0 = m.rank[ra] + (uint32_t)(m.rs[ra] & 1ull) - 1u;
+		const uint32_t k1 = m.rank[rb] + (uint32_t)__popcll(m.rs[rb] & (~0ull >> (63 - a))) - 1u;
+		const uint32_t k2 = m.rank[rc] + (uint32_t)__popcll(m.rs[rc] & (~0ull >> (63 - a))) - 1u;
+		const uint32_t w0 = __ldg(stream + (s0 ? k0 : 0u)), w1 = __ldg(stream + (s1 ? k1 : 0u));
+		const uint32_t w2 = __ldg(stream + (s2 ? k2 : 0u));
+		cols[i] = s0 ? (uint8_t)(w0 >> 24) : (uint8_t)0;
+		cols[RR + i] = s1 ? (uint8_t)(w1 >> 24) : (uint8_t)0;
+		cols[2 * RR + i] = s2 ? (uint8_t)(w2 >> 24) : (uint8_t)0;
 	}
 	if (ds != kNoSlot) store_decoded_wait();
 }
