@@ -547,17 +547,6 @@ def run_ours(args):
         if not args.skip_full_scale:
             fs = full_scale(ctx)
             res5, dw5 = fs.pop("_res"), fs.pop("_dw")
-            rle5 = dw5.rle_bytes()
-            # step bytes: RLE in, splats out plus the grouped copy of levels
-            # >= 1 (read and written again), mesh out, the shadow map once
-            ab5 = rle5 + int(res5["svl_total"].astype(np.int64).sum()) * 2 \
-                + int(res5["svl_items"][:, 1:].astype(np.int64).sum()) * 2 * 2 \
-                + int(res5["vbo_items"].astype(np.int64).sum()) * 2 + int(res5["ibo_items"].astype(np.int64).sum()) * 4 \
-                + 16896 * 16384 * 2
-            fs["rle_gb"] = round(rle5 / 1e9, 3)
-            fs["step_bytes"] = int(ab5)
-            fs["step_gbs"] = round(ab5 / (fs["ms_per_rebuild"] / 1e3) / 1e9, 1)
-            fs["step_frac_of_measured_hbm"] = round(fs["step_gbs"] / peaks()[0], 4)
             fs["draw_cull"] = draw_cull(dw5)
             dw5.close()
             detail["full_scale"] = fs
@@ -833,6 +822,15 @@ def full_scale(ctx, steps=3, bits=(8, 8)):
     ctx.set_timing(False)
     splats = int(res["svl_total"].astype(np.int64).sum()) // 4
     faces = int(res["ibo_items"].astype(np.int64).sum()) // 6
+    # step bytes: RLE in, splats out plus the grouped copy of levels >= 1
+    # (read and written again), mesh out, the shadow map once ((X + Y) x Z
+    # entries of 2 bytes)
+    rle = dw.rle_bytes()
+    grouped = int(res["svl_items"][:, 1:].astype(np.int64).sum()) * 2
+    geo_out = int(res["svl_total"].astype(np.int64).sum()) * 2 + int(res["vbo_items"].astype(np.int64).sum()) * 2 \
+        + int(res["ibo_items"].astype(np.int64).sum()) * 4
+    shadow_b = ((64 << bx) + 512) * (64 << bz) * 2
+    step_b = rle + geo_out + 2 * grouped + shadow_b
     out = {
         "workload": "%dx512x%d world (%dx8x%d = %d chunks of 64^3), terrain+caves at 4x horizontal "
                     "noise scale, RLE-resident; LOD 0..5, splats/meshes, LOD/octree grouping"
@@ -851,6 +849,11 @@ def full_scale(ctx, steps=3, bits=(8, 8)):
         "faces": faces,
         "mesh_chunks": int(modes.sum()),
         "world_gen_s": round(gen_s, 2),
+        "rle_gb": round(rle / 1e9, 3),
+        "bytes_split": {"rle_in": rle, "geometry_out": geo_out, "grouped_copy": 2 * grouped, "shadow_map": shadow_b},
+        "step_bytes": int(step_b),
+        "step_gbs": round(step_b / (ms / 1e3) / 1e9, 1),
+        "step_frac_of_measured_hbm": round(step_b / (ms / 1e3) / 1e9 / peaks()[0], 4),
     }
     out["_res"] = res
     out["_dw"] = dw
