@@ -17,9 +17,9 @@
  * is a bijection onto [0, nchunks): the prefix sum of the level-l item
  * counts in key order gives every segment's destination, and node i's
  * buffer starts at the prefix of its first key. One pass scatters counts
- * into key order, one CTA per level scans them, and a CTA per chunk copies
- * its segment with 8-byte vector moves (one splat per thread per step) into
- * the group arena, levels 1, 2, ... one after the other.
+ * into key order, one CTA per level scans them, and a warp per segment
+ * copies it with 8-byte vector moves (one splat per lane per step, eight
+ * loads in flight per lane) into the group arena.
  *
  * A rebuild whose splat arena overflowed left some chunks without lists
  * (their records carry the overflow status); the copy is then skipped as a
@@ -161,7 +161,17 @@ __global__ void __launch_bounds__(256) k_group_copy(const ChunkOut *__restrict__
 		if (src_off + items > a.svl_cap_units * 8u || dst_off + items > a.out_cap) continue;
 		const uint2 *src = (const uint2 *)(a.svl + src_off);
 		uint2 *dst = (uint2 *)(a.out + dst_off);
-		for (uint32_t s = lane; s < items / 4u; s += 32u) dst[s] = __ldg(src + s);
+		const uint32_t n = items / 4u;
+		/* eight loads in flight per lane before their stores */
+		uint32_t s = lane;
+		for (; s + 224u < n; s += 256u) {
+			uint2 v[8];
+#pragma unroll
+			for (int u = 0; u < 8; u++) v[u] = __ldg(src + s + 32u * u);
+#pragma unroll
+			for (int u = 0; u < 8; u++) dst[s + 32u * u] = v[u];
+		}
+		for (; s < n; s += 32u) dst[s] = __ldg(src + s);
 	}
 }
 
