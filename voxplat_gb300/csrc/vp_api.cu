@@ -280,6 +280,7 @@ VP_API void vp_world_destroy(vp_world *w)
 	if (w->h_check) cudaFreeHost(w->h_check);
 	dev_free(w->d_set);
 	dev_free(w->d_items);
+	dev_free(w->d_shell_items);
 	dev_free(w->d_outs);
 	dev_free(w->d_queue);
 	dev_free(w->d_cursors);
@@ -566,6 +567,7 @@ VP_API int vp_world_set_handoff(vp_world *w, int on)
 		dev_free(w->d_dec);
 		dev_free(w->d_dec_slot);
 		w->dec_bytes = 0;
+		w->h_dec_slot.clear();
 	}
 	return VP_OK;
 }
@@ -585,8 +587,34 @@ VP_API int vp_world_set_modes(vp_world *w, const uint8_t *make_mesh)
 	return VP_OK;
 }
 
+/* The shell pass of a full rebuild: the decoding shell kernel over the
+ * chunks of more than one run, the single-run ones without decoding (<=
+ * 64^3; the 128^3 shell kernel is persistent and takes every chunk). Call
+ * after ensure_items. */
+static void set_shell_items(vp_world *w, GeoLaunch &L)
+{
+	if (w->root_bitw <= 6 && w->d_shell_items) {
+		L.shell_items = w->d_shell_items;
+		L.n_shell = w->n_shell_multi;
+		L.uni_items = w->d_shell_items + w->n_shell_multi;
+		L.n_uni = w->nchunks - w->n_shell_multi;
+	} else {
+		L.shell_items = w->d_items;
+		L.n_shell = w->nchunks;
+	}
+}
+
 static int ensure_items(vp_world *w)
 {
+	if (w->lens_stale) {
+		/* edits re-encoded streams on the device: refresh the lengths the
+		 * work orders are built from */
+		w->hlen.resize(w->nchunks);
+		CK(cudaMemcpyAsync(w->hlen.data(), w->d_len, w->nchunks * 4u, cudaMemcpyDeviceToHost, w->ctx->stream));
+		CK(cudaStreamSynchronize(w->ctx->stream));
+		w->lens_stale = false;
+		w->items_dirty = true;
+	}
 	if (!w->items_dirty) return VP_OK;
 	/* longest first: a chunk's cost grows with its run count, and a meshed
 	 * chunk costs about three times a splatted one */
@@ -610,6 +638,31 @@ static int ensure_items(vp_world *w)
 			   w->ctx->stream));
 	CK(cudaStreamSynchronize(w->ctx->stream));
 	w->h_items.swap(it);
+	/* shell order: chunks of more than one run, and any chunk with a
+	 * handoff slot (the shell pass stores its decoded state), longest
+	 * first; then the single-run chunks */
+	{
+		std::vector<uint32_t> multi, uni;
+		for (uint32_t c = 0; c < w->nchunks; c++) {
+			const uint32_t len = c < w->hlen.size() ? w->hlen[c] : 2u;
+			const bool slot = c < w->h_dec_slot.size() && w->h_dec_slot[c] != kNoSlot;
+			(len > 2u || slot ? multi : uni).push_back(c);
+		}
+		std::stable_sort(multi.begin(), multi.end(), [&](uint32_t a, uint32_t b) {
+			const uint32_t la = a < w->hlen.size() ? w->hlen[a] : 2u, lb = b < w->hlen.size() ? w->hlen[b] : 2u;
+			return la > lb;
+		});
+		std::vector<WorkItem> sh;
+		sh.reserve(w->nchunks);
+		for (uint32_t c : multi) sh.push_back(WorkItem{0u, c, 0u, c});
+		for (uint32_t c : uni) sh.push_back(WorkItem{0u, c, 0u, c});
+		int rc;
+		if (!w->d_shell_items && (rc = dev_alloc(&w->d_shell_items, w->nchunks))) return rc;
+		CK(cudaMemcpyAsync(w->d_shell_items, sh.data(), sh.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
+				   w->ctx->stream));
+		CK(cudaStreamSynchronize(w->ctx->stream));
+		w->n_shell_multi = (uint32_t)multi.size();
+	}
 	w->items_dirty = false;
 	w->stream_slabs = 0; /* the slab orders follow the work order */
 	return VP_OK;
@@ -647,6 +700,7 @@ uint8_t *vpi_decoded(vp_world *w)
 		return nullptr;
 	}
 	w->dec_bytes = need;
+	w->h_dec_slot.swap(slot);
 	return w->d_dec;
 }
 
@@ -736,8 +790,7 @@ static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 	L.sets = w->d_set;
 	L.items = w->d_items;
 	L.n_items = w->nchunks;
-	L.shell_items = w->d_items;
-	L.n_shell = w->nchunks;
+	set_shell_items(w, L);
 	L.threads = 512;
 	L.outs = w->d_outs;
 	L.lod_max = lod_max;
@@ -1227,8 +1280,7 @@ static int stream_rebuild(vp_world *w, int lod_max, unsigned flags, int slabs, v
 	L.big_scratch = w->d_big;
 	L.big_slots = w->big_slots;
 	L.sets = w->d_set;
-	L.shell_items = w->d_items;
-	L.n_shell = w->nchunks;
+	set_shell_items(w, L);
 	L.threads = 512;
 	L.outs = w->d_outs;
 	L.lod_max = lod_max;

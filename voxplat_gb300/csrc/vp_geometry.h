@@ -10,6 +10,10 @@ struct GeoLaunch {
 	uint32_t n_items;
 	const WorkItem *shell_items;/* device array: chunks whose shell to write */
 	uint32_t n_shell;
+	/* <= 64^3 chunks: single-run chunks (one run and the terminator) whose
+	 * shells, unless all air, the shell pass writes without decoding */
+	const WorkItem *uni_items;
+	uint32_t n_uni;
 	int run_shell;
 	unsigned int *queue;        /* device counter for persistent CTAs, or NULL */
 	uint32_t ctas;              /* persistent grid size */

@@ -443,6 +443,32 @@ __global__ void __launch_bounds__(512, 2) k_shell(const SetDesc *__restrict__ se
 	if (ds != kNoSlot) store_decoded_wait();
 }
 
+/* Shells of single-run chunks (one run of R^3 voxels and the terminator),
+ * without decoding: an all-air chunk has none (its neighbours see air); a
+ * solid one has every boundary bit set and its run's colour on the three
+ * low planes, as k_shell would write them. One warp per chunk; a chunk of
+ * more than one run is left to k_shell. */
+template <int RB>
+__global__ void __launch_bounds__(256) k_shell_uniform(const SetDesc *__restrict__ sets,
+						       const WorkItem *__restrict__ items, uint32_t nitems)
+{
+	using G = Geo<RB>;
+	constexpr uint32_t N = (uint32_t)G::R * G::R * G::R;
+	const uint32_t it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const int lane = threadIdx.x & 31;
+	if (it >= nitems) return;
+	const WorkItem wi = items[it];
+	const SetDesc *S = sets + wi.set;
+	if (S->len[wi.chunk] != 2u) return;
+	const uint32_t w0 = S->pool[S->off[wi.chunk]];
+	if (w0 == N) return;
+	uint64_t *bits = S->shell_bits + (size_t)wi.chunk * G::shell_words;
+	for (int i = lane; i < (int)G::shell_words; i += 32) bits[i] = G::MASK;
+	uint32_t *cols = (uint32_t *)(S->shell_col + (size_t)wi.chunk * G::shell_cols);
+	const uint32_t c4 = (w0 >> 24) * 0x01010101u;
+	for (int i = lane; i < (int)(G::shell_cols / 4); i += 32) cols[i] = c4;
+}
+
 /* ------------------------------------------------------------------ */
 /* Geometry pass                                                       */
 /* ------------------------------------------------------------------ */
@@ -1549,6 +1575,11 @@ static cudaError_t launch_rb(const GeoLaunch &L, cudaStream_t st)
 	if (L.run_shell && L.n_shell) {
 		k_shell<RB><<<L.n_shell, L.threads, G::bytes, st>>>(L.sets, L.shell_items, L.n_shell, L.decoded,
 								     L.dec_slot);
+		e = cudaGetLastError();
+		if (e != cudaSuccess) return e;
+	}
+	if (L.run_shell && L.n_uni) {
+		k_shell_uniform<RB><<<(L.n_uni + 7) / 8, 256, 0, st>>>(L.sets, L.uni_items, L.n_uni);
 		e = cudaGetLastError();
 		if (e != cudaSuccess) return e;
 	}

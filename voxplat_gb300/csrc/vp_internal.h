@@ -79,6 +79,7 @@ struct vp_world {
 	uint64_t shadow_cap = 0;                 /* elements allocated in d_shadow */
 	uint8_t *d_dec = nullptr;                /* decoded chunks, shell pass -> geometry pass */
 	uint32_t *d_dec_slot = nullptr;          /* per chunk: its slot in d_dec, or kNoSlot */
+	std::vector<uint32_t> h_dec_slot;        /* host copy */
 	size_t dec_bytes = 0;
 	bool dec_failed = false;                 /* no room: rebuilds decode twice */
 	bool handoff = true;                     /* vp_world_set_handoff */
@@ -129,8 +130,14 @@ struct vp_world {
 	uint32_t big_slots = 0;
 	SetDesc *d_set = nullptr;
 	WorkItem *d_items = nullptr;
+	/* shell pass order: the chunks of more than one run (or with a handoff
+	 * slot), longest first, then the single-run chunks, whose shells (if
+	 * not all air) k_shell_uniform writes */
+	WorkItem *d_shell_items = nullptr;
+	uint32_t n_shell_multi = 0;
 	std::vector<uint8_t> modes;
 	std::vector<uint32_t> hlen;              /* host copy of stream lengths */
+	bool lens_stale = false;                 /* an edit changed lengths on the device since hlen */
 	bool items_dirty = true;
 	ChunkOut *d_outs = nullptr;
 	unsigned int *d_queue = nullptr;

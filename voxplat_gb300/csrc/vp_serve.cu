@@ -418,6 +418,7 @@ int enqueue_batch(vp_world *w, EditSlot *s, const vp_edit *edits, uint32_t n, co
 	e = launch_rle_encode_tiles(s->d_vols, nd, N, w->d_pool, w->pool_cap, w->d_pool_cursor, s->d_new_off, s->d_new_len,
 				    (uint32_t *)s->d_status, s->d_tile, s->d_nruns, s->d_runs, st);
 	if (e == cudaSuccess) e = launch_scatter_streams(s->d_dirty, nd, s->d_new_off, s->d_new_len, 0, w->d_off, w->d_len, st);
+	w->lens_stale = true; /* the full rebuilds' work orders follow the new lengths */
 	if (e != cudaSuccess) return cuda_fail(e, "edit re-encode");
 	w->pool_version++;
 	CK(cudaMemcpyAsync(s->h_pin, w->d_pool_cursor, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
