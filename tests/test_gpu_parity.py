@@ -114,24 +114,28 @@ def test_edge_cases(ctx, name):
 def test_single_run_chunk_shells(ctx):
     """All-air and one-colour chunks (one run each) next to chunks of many
     runs: the shell pass writes the one-colour chunks' shells without
-    decoding and skips the air ones. Then edits turn an air chunk and a
-    one-colour chunk into many-run chunks (and the work orders follow the
-    new lengths) before a full rebuild."""
+    decoding and skips the air ones, and an air chunk with only air beyond
+    its +x, +y and +z faces gets a zeroed result record without a geometry
+    pass. Then edits turn two air chunks (one of them that one) and a
+    one-colour chunk into many-run chunks (the work orders follow the new
+    lengths) before a full rebuild."""
     R = 16
     rng = np.random.default_rng(12)
     air = np.zeros(R ** 3, np.uint8)
     noise = rng.integers(1, 256, R ** 3).astype(np.uint8)
     noise[rng.random(R ** 3) < 0.6] = 0
+    # chunk 7 (the +x +y +z corner) is air with nothing beyond it: no geometry
     vox = [air, np.full(R ** 3, 200, np.uint8), noise, np.full(R ** 3, 13, np.uint8),
-           noise[::-1].copy(), air, np.full(R ** 3, 200, np.uint8), noise]
+           noise[::-1].copy(), air, np.full(R ** 3, 200, np.uint8), air]
     w = worlds.world_from_voxels(4, (1, 1, 1), vox)
     w.shadow[:w.shadow_w * w.shadow_z] = rng.integers(0, 40, w.shadow_w * w.shadow_z)
     o = OracleWorld(w)
     dw = gpu.DeviceWorld(ctx, w)
     for modes in (None, np.ones(8, np.uint8), (np.arange(8) % 2).astype(np.uint8)):
         assert worlds.compare_world(dw, o, modes, 4) == [], modes
-    # a sphere into the air chunk 0, a hole in the one-colour chunk 1
-    batch = [(8, 8, 8, 5, 90), (24, 8, 8, 4, 0)]
+    # a sphere into the air chunk 0 and into the chunk without geometry,
+    # a hole in the one-colour chunk 1
+    batch = [(8, 8, 8, 5, 90), (24, 24, 24, 5, 77), (24, 8, 8, 4, 0)]
     for e in batch:
         o.edit_sphere(e[:3], e[3], e[4])
     dw.edit(gpu.make_edits(batch))

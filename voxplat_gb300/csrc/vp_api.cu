@@ -281,6 +281,7 @@ VP_API void vp_world_destroy(vp_world *w)
 	dev_free(w->d_set);
 	dev_free(w->d_items);
 	dev_free(w->d_shell_items);
+	dev_free(w->d_null);
 	dev_free(w->d_outs);
 	dev_free(w->d_queue);
 	dev_free(w->d_cursors);
@@ -447,6 +448,8 @@ VP_API int vp_world_upload(vp_world *w, const uint32_t *pool, uint64_t pool_word
 	}
 	w->pool_words = total;
 	w->hlen.assign(len, len + w->nchunks);
+	w->hnull.resize(w->nchunks);
+	for (uint32_t c = 0; c < w->nchunks; c++) w->hnull[c] = (len[c] == 2u && pool[off[c]] == N) ? 1u : 0u;
 	w->items_dirty = true;
 	w->shadow_len = shadow_len;
 	w->shadow_w = shadow_w;
@@ -549,6 +552,7 @@ VP_API int vp_world_generate(vp_world *w, int kind, uint64_t seed, int hshift, u
 	w->hlen.resize(w->nchunks);
 	CK(cudaMemcpyAsync(w->hlen.data(), w->d_len, w->nchunks * 4u, cudaMemcpyDeviceToHost, st));
 	CK(cudaStreamSynchronize(st));
+	w->hnull.clear();
 	w->uploaded = true;
 	w->items_dirty = true;
 	return vpi_upload_setdesc(w);
@@ -587,6 +591,13 @@ VP_API int vp_world_set_modes(vp_world *w, const uint8_t *make_mesh)
 	return VP_OK;
 }
 
+/* flags[c] = 1 when chunk c is all air (one air run and the terminator) */
+__global__ void k_null_flags(const SetDesc *__restrict__ set, uint32_t n, uint32_t N, uint8_t *flags)
+{
+	const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+	if (c < n) flags[c] = (set->len[c] == 2u && set->pool[set->off[c]] == N) ? 1u : 0u;
+}
+
 /* The shell pass of a full rebuild: the decoding shell kernel over the
  * chunks of more than one run, the single-run ones without decoding (<=
  * 64^3; the 128^3 shell kernel is persistent and takes every chunk). Call
@@ -613,19 +624,53 @@ static int ensure_items(vp_world *w)
 		CK(cudaMemcpyAsync(w->hlen.data(), w->d_len, w->nchunks * 4u, cudaMemcpyDeviceToHost, w->ctx->stream));
 		CK(cudaStreamSynchronize(w->ctx->stream));
 		w->lens_stale = false;
+		w->hnull.clear();
 		w->items_dirty = true;
 	}
 	if (!w->items_dirty) return VP_OK;
+	/* which chunks are all air (known on the host after an upload; after a
+	 * generation, a file load or edits, read from the device once) */
+	if (w->hnull.size() != w->nchunks) {
+		int rc0;
+		if (!w->d_null && (rc0 = dev_alloc(&w->d_null, w->nchunks))) return rc0;
+		w->hnull.resize(w->nchunks);
+		k_null_flags<<<(w->nchunks + 255) / 256, 256, 0, w->ctx->stream>>>(w->d_set, w->nchunks,
+										    1u << (3 * w->root_bitw), w->d_null);
+		CK(cudaGetLastError());
+		CK(cudaMemcpyAsync(w->hnull.data(), w->d_null, w->nchunks, cudaMemcpyDeviceToHost, w->ctx->stream));
+		CK(cudaStreamSynchronize(w->ctx->stream));
+	}
+	/* those whose +x, +y and +z neighbours are all air (or outside) too
+	 * have no geometry */
+	const std::vector<uint8_t> &null = w->hnull;
+	const uint32_t bx = w->max_bitw[0], by = w->max_bitw[1], bz = w->max_bitw[2];
+	auto air = [&](uint32_t c, int dx, int dy, int dz) {
+		const uint32_t x = (c & ((1u << bx) - 1u)) + dx, y = ((c >> bx) & ((1u << by) - 1u)) + dy,
+			       z = (c >> (bx + by)) + dz;
+		if (x >> bx || y >> by || z >> bz) return true; /* outside the world */
+		return null[(z << (bx + by)) | (y << bx) | x] != 0;
+	};
 	/* longest first: a chunk's cost grows with its run count, and a meshed
-	 * chunk costs about three times a splatted one */
+	 * chunk costs about three times a splatted one; chunks without geometry
+	 * last */
 	std::vector<uint32_t> order(w->nchunks);
 	std::vector<uint64_t> cost(w->nchunks);
+	uint32_t n_geo = 0;
 	for (uint32_t c = 0; c < w->nchunks; c++) {
 		order[c] = c;
 		const uint64_t len = c < w->hlen.size() ? w->hlen[c] : 2u;
-		cost[c] = (len + 64u) * (w->modes[c] ? 3u : 1u);
+		/* (a chunk holding a handoff slot is in the decoding shell list,
+		 * which does not zero records: it keeps its geometry pass) */
+		const bool slot = c < w->h_dec_slot.size() && w->h_dec_slot[c] != kNoSlot;
+		const bool empty = w->root_bitw <= 6 && !slot && null[c] && air(c, 1, 0, 0) && air(c, 0, 1, 0) &&
+				   air(c, 0, 0, 1);
+		cost[c] = empty ? 0u : (len + 64u) * (w->modes[c] ? 3u : 1u);
+		n_geo += empty ? 0u : 1u;
 	}
 	std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
+	w->n_geo = n_geo;
+	std::vector<uint8_t> no_geometry(w->nchunks, 0);
+	for (uint32_t k = n_geo; k < w->nchunks; k++) no_geometry[order[k]] = 1;
 	std::vector<WorkItem> it(w->nchunks);
 	for (uint32_t k = 0; k < w->nchunks; k++) {
 		const uint32_t c = order[k];
@@ -655,7 +700,7 @@ static int ensure_items(vp_world *w)
 		std::vector<WorkItem> sh;
 		sh.reserve(w->nchunks);
 		for (uint32_t c : multi) sh.push_back(WorkItem{0u, c, 0u, c});
-		for (uint32_t c : uni) sh.push_back(WorkItem{0u, c, 0u, c});
+		for (uint32_t c : uni) sh.push_back(WorkItem{0u, c, no_geometry[c] ? kItemEmpty : 0u, c});
 		int rc;
 		if (!w->d_shell_items && (rc = dev_alloc(&w->d_shell_items, w->nchunks))) return rc;
 		CK(cudaMemcpyAsync(w->d_shell_items, sh.data(), sh.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
@@ -861,6 +906,7 @@ static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 		if (ctx->timing) cudaEventRecord(e1, st);
 		GeoLaunch Lg = L;
 		Lg.run_shell = 0;
+		Lg.n_items = w->n_geo;
 		e = launch_geometry(w->root_bitw, Lg, st);
 		if (e != cudaSuccess) return cuda_fail(e, "geometry launch");
 		w->launches += 2;
@@ -1265,13 +1311,13 @@ static int stream_rebuild(vp_world *w, int lod_max, unsigned flags, int slabs, v
 		std::vector<WorkItem> order;
 		order.reserve(w->nchunks);
 		for (int k = 0; k < slabs; k++)
-			for (uint32_t i = (uint32_t)k; i < w->nchunks; i += (uint32_t)slabs) order.push_back(w->h_items[i]);
+			for (uint32_t i = (uint32_t)k; i < w->n_geo; i += (uint32_t)slabs) order.push_back(w->h_items[i]);
 		CK(cudaMemcpyAsync(w->d_stream_items, order.data(), order.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
 				   st));
 		CK(cudaStreamSynchronize(st));
 		w->stream_slabs = slabs;
 	}
-	for (int k = 0; k < slabs; k++) first[k + 1] = first[k] + (w->nchunks - (uint32_t)k + (uint32_t)slabs - 1) / slabs;
+	for (int k = 0; k < slabs; k++) first[k + 1] = first[k] + (w->n_geo - (uint32_t)k + (uint32_t)slabs - 1) / slabs;
 	k_put_cursors<<<1, 32, 0, st>>>(w->d_cursors, base[0], base[1], base[2]);
 	CK(cudaGetLastError());
 	CK(cudaMemsetAsync(w->d_slab_q, 0, kMaxStreamSlabs * sizeof(unsigned int), st));
@@ -1571,6 +1617,7 @@ int vpi_world_load(vp_world *w, const VpiChunkSrc *src)
 	CK(cudaMemcpyAsync(w->d_off, off.data(), w->nchunks * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
 	CK(cudaMemcpyAsync(w->d_len, len.data(), w->nchunks * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
 	w->hlen = len;
+	w->hnull.clear();
 	w->pool_words = total;
 	w->pool_cap = total;
 	w->pool_tail = total;
@@ -1609,6 +1656,7 @@ int vpi_world_run(vp_world *w, const WorkItem *items, uint32_t n, int lod_max)
 		std::vector<WorkItem> all(w->nchunks);
 		for (uint32_t c = 0; c < w->nchunks; c++) all[c] = WorkItem{0, c, 0, c};
 		CK(cudaMemcpyAsync(w->d_items, all.data(), all.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, st));
+		w->items_dirty = true; /* the full rebuilds' work order is rebuilt before the next one */
 		WorkItem *d_run = nullptr;
 		if ((rc = dev_alloc(&d_run, n))) return rc;
 		cudaMemcpyAsync(d_run, items, n * sizeof(WorkItem), cudaMemcpyHostToDevice, st);

@@ -40,7 +40,7 @@ struct SetDesc {
 };
 
 /* flags of a work item */
-enum : uint32_t { kItemMesh = 1u, kItemMaskDense = 2u };
+enum : uint32_t { kItemMesh = 1u, kItemMaskDense = 2u, kItemEmpty = 4u /* shell list: no geometry, zero the record */ };
 
 struct WorkItem {
 	uint32_t set;

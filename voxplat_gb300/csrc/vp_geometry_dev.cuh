@@ -447,10 +447,13 @@ __global__ void __launch_bounds__(512, 2) k_shell(const SetDesc *__restrict__ se
  * without decoding: an all-air chunk has none (its neighbours see air); a
  * solid one has every boundary bit set and its run's colour on the three
  * low planes, as k_shell would write them. One warp per chunk; a chunk of
- * more than one run is left to k_shell. */
+ * more than one run is left to k_shell. An item flagged kItemEmpty (all
+ * air, with all-air or no +x, +y and +z neighbours) gets no geometry pass:
+ * its result record is zeroed here, as the geometry pass would write it. */
 template <int RB>
 __global__ void __launch_bounds__(256) k_shell_uniform(const SetDesc *__restrict__ sets,
-						       const WorkItem *__restrict__ items, uint32_t nitems)
+						       const WorkItem *__restrict__ items, uint32_t nitems,
+						       ChunkOut *outs)
 {
 	using G = Geo<RB>;
 	constexpr uint32_t N = (uint32_t)G::R * G::R * G::R;
@@ -458,6 +461,12 @@ __global__ void __launch_bounds__(256) k_shell_uniform(const SetDesc *__restrict
 	const int lane = threadIdx.x & 31;
 	if (it >= nitems) return;
 	const WorkItem wi = items[it];
+	if (wi.flags & kItemEmpty) {
+		static_assert(sizeof(ChunkOut) % 4 == 0, "result records are whole words");
+		uint32_t *o = (uint32_t *)(outs + wi.slot);
+		for (int i = lane; i < (int)(sizeof(ChunkOut) / 4); i += 32) o[i] = 0u;
+		return;
+	}
 	const SetDesc *S = sets + wi.set;
 	if (S->len[wi.chunk] != 2u) return;
 	const uint32_t w0 = S->pool[S->off[wi.chunk]];
@@ -1579,7 +1588,7 @@ static cudaError_t launch_rb(const GeoLaunch &L, cudaStream_t st)
 		if (e != cudaSuccess) return e;
 	}
 	if (L.run_shell && L.n_uni) {
-		k_shell_uniform<RB><<<(L.n_uni + 7) / 8, 256, 0, st>>>(L.sets, L.uni_items, L.n_uni);
+		k_shell_uniform<RB><<<(L.n_uni + 7) / 8, 256, 0, st>>>(L.sets, L.uni_items, L.n_uni, L.outs);
 		e = cudaGetLastError();
 		if (e != cudaSuccess) return e;
 	}

@@ -130,6 +130,12 @@ struct vp_world {
 	uint32_t big_slots = 0;
 	SetDesc *d_set = nullptr;
 	WorkItem *d_items = nullptr;
+	/* d_items[0, n_geo): chunks with geometry to build, longest first;
+	 * [n_geo, nchunks): chunks that are all air with all-air (or no) +x, +y
+	 * and +z neighbours, whose result records a rebuild only zeroes */
+	uint32_t n_geo = 0;
+	uint8_t *d_null = nullptr;               /* per chunk: 1 = all air (one air run) */
+	std::vector<uint8_t> hnull;              /* host copy; empty = to be fetched */
 	/* shell pass order: the chunks of more than one run (or with a handoff
 	 * slot), longest first, then the single-run chunks, whose shells (if
 	 * not all air) k_shell_uniform writes */
