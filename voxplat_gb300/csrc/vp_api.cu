@@ -872,6 +872,7 @@ static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 			Ls.n_items = 0;
 			Ls.shell_items = w->d_items + k;
 			Ls.n_shell = 1;
+			Ls.n_uni = 0; /* every chunk its own shell launch, single-run ones too */
 			Ls.run_shell = 1;
 			if (conc && w->root_bitw == 7) { /* a scratch slot per stream */
 				Ls.big_scratch = w->d_big + (size_t)(k % kPlainStreams) * big_scratch_slot_bytes();
