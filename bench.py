@@ -916,6 +916,8 @@ def main():
     ap.add_argument("--uneven-only", type=int, nargs=2, metavar=("ROOT_BITW", "N"),
                     help="run only the mixed-root batch, restricted to its first N chunks of one root "
                          "(a small case for profiling); prints that sub-benchmark's line")
+    ap.add_argument("--edits-only", action="store_true",
+                    help="run only the edit-serving sub-benchmark; prints its line")
     ap.add_argument("--full-scale-only", type=int, nargs=2, metavar=("BITS_X", "BITS_Z"),
                     help="run only the full-scale rebuild, on the corner of its world 2^BITS_X x 8 x 2^BITS_Z "
                          "chunks (8 8 is the full world); prints that sub-benchmark's line")
@@ -926,6 +928,10 @@ def main():
         from voxplat_gb300 import gpu
         root, n = args.uneven_only
         print(json.dumps(uneven_batch(gpu.Context(0), n=n, root=root)), flush=True)
+        return
+    if args.edits_only:
+        from voxplat_gb300 import gpu
+        print(json.dumps(edit_serving(gpu.Context(0))), flush=True)
         return
     if args.full_scale_only:
         from voxplat_gb300 import gpu
