@@ -282,6 +282,8 @@ VP_API void vp_world_destroy(vp_world *w)
 	dev_free(w->d_items);
 	dev_free(w->d_shell_items);
 	dev_free(w->d_null);
+	dev_free(w->d_pool_spare);
+	dev_free(w->d_noff);
 	dev_free(w->d_outs);
 	dev_free(w->d_queue);
 	dev_free(w->d_cursors);

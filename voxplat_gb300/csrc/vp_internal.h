@@ -162,6 +162,12 @@ struct vp_world {
 	int32_t origin[3] = {0, 0, 0};           /* world chunk coords of chunk 0 */
 	/* edits: the pool grows at its tail, re-encoded streams are appended */
 	uint64_t pool_cap = 0;                   /* words allocated in d_pool */
+	/* the edit server's pool compaction copies into this spare pool and
+	 * keeps the old one as the next spare: no device allocation while
+	 * serving (set up with the server) */
+	uint32_t *d_pool_spare = nullptr;
+	uint64_t pool_spare_cap = 0;
+	uint64_t *d_noff = nullptr;              /* compaction scratch, nchunks offsets */
 	uint64_t pool_tail = 0;                  /* first free word */
 	unsigned long long *d_pool_cursor = nullptr; /* device copy of the pool tail while edit batches append */
 	EditSlot *eslot = nullptr;               /* the synchronous edit path's batch state (vp_world_edit) */

@@ -111,26 +111,40 @@ int compact_pool(vp_world *w, uint64_t extra_words)
 		noff[c] = total;
 		total += (len[c] + 3u) & ~3u;
 	}
-	const uint64_t cap = total + total / 4 + extra_words + (16u << 20);
+	uint64_t cap = total + total / 4 + extra_words + (16u << 20);
 	uint32_t *np = nullptr;
-	uint64_t *d_noff = nullptr;
-	int rc = dev_alloc(&np, cap);
-	if (!rc) rc = dev_alloc(&d_noff, w->nchunks);
-	if (rc) {
+	int rc;
+	if (w->d_pool_spare && w->pool_spare_cap >= cap) {
+		/* the spare pool holds it: no allocation */
+		np = w->d_pool_spare;
+		cap = w->pool_spare_cap;
+		w->d_pool_spare = nullptr;
+		w->pool_spare_cap = 0;
+	} else if ((rc = dev_alloc(&np, cap))) {
+		return rc;
+	}
+	if (!w->d_noff && (rc = dev_alloc(&w->d_noff, w->nchunks))) {
 		dev_free(np);
 		return rc;
 	}
-	cudaError_t e = cudaMemcpyAsync(d_noff, noff.data(), w->nchunks * 8u, cudaMemcpyHostToDevice, st);
-	if (e == cudaSuccess) e = launch_copy_streams(w->d_pool, w->d_off, w->d_len, d_noff, np, w->nchunks, st);
-	if (e == cudaSuccess) e = cudaMemcpyAsync(w->d_off, d_noff, w->nchunks * 8u, cudaMemcpyDeviceToDevice, st);
+	cudaError_t e = cudaMemcpyAsync(w->d_noff, noff.data(), w->nchunks * 8u, cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess) e = launch_copy_streams(w->d_pool, w->d_off, w->d_len, w->d_noff, np, w->nchunks, st);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(w->d_off, w->d_noff, w->nchunks * 8u, cudaMemcpyDeviceToDevice, st);
 	w->pool_version++;
 	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-	dev_free(d_noff);
 	if (e != cudaSuccess) {
 		dev_free(np);
 		return cuda_fail(e, "pool compaction");
 	}
-	dev_free(w->d_pool);
+	/* the old pool is the next spare (a smaller one than the spare it
+	 * replaces is freed) */
+	if (w->pool_cap >= w->pool_spare_cap) {
+		dev_free(w->d_pool_spare);
+		w->d_pool_spare = w->d_pool;
+		w->pool_spare_cap = w->pool_cap;
+	} else {
+		dev_free(w->d_pool);
+	}
 	w->d_pool = np;
 	w->pool_cap = cap;
 	w->pool_tail = total;
@@ -868,6 +882,15 @@ VP_API int vp_server_create(vp_world *w, const vp_server_config *cfg, vp_server 
 			return rc == VP_ECUDA || rc == VP_ENOMEM ? VP_ENOMEM : rc;
 		}
 	}
+	/* a spare pool for compactions while serving (without the room, a
+	 * compaction allocates one then) */
+	const uint64_t spare = w->pool_cap + w->pool_cap / 4 + (16u << 20);
+	if (w->pool_spare_cap < spare && free_b > cfg->hbm_reserve + spare * 4u + nslots * per) {
+		dev_free(w->d_pool_spare);
+		w->pool_spare_cap = 0;
+		if (dev_alloc(&w->d_pool_spare, spare) == VP_OK) w->pool_spare_cap = spare;
+	}
+	if (!w->d_noff && dev_alloc(&w->d_noff, w->nchunks) != VP_OK) w->d_noff = nullptr;
 	s->t0 = now_s();
 	s->tail_known = w->pool_tail;
 	w->server = s;
