@@ -449,10 +449,15 @@ VP_API int vp_world_upload(vp_world *w, const uint32_t *pool, uint64_t pool_word
 		return VP_EINVAL;
 	}
 	w->pool_words = total;
+	/* the work orders depend on the lengths and on which chunks are all
+	 * air: an upload that changes neither keeps them */
+	std::vector<uint8_t> null(w->nchunks);
+	for (uint32_t c = 0; c < w->nchunks; c++) null[c] = (len[c] == 2u && pool[off[c]] == N) ? 1u : 0u;
+	const bool same = w->hlen.size() == w->nchunks && std::equal(len, len + w->nchunks, w->hlen.begin()) &&
+			  w->hnull == null && !w->lens_stale;
 	w->hlen.assign(len, len + w->nchunks);
-	w->hnull.resize(w->nchunks);
-	for (uint32_t c = 0; c < w->nchunks; c++) w->hnull[c] = (len[c] == 2u && pool[off[c]] == N) ? 1u : 0u;
-	w->items_dirty = true;
+	w->hnull.swap(null);
+	if (!same) w->items_dirty = true;
 	w->shadow_len = shadow_len;
 	w->shadow_w = shadow_w;
 	w->uploaded = true;
