@@ -1514,7 +1514,12 @@ __global__ void __launch_bounds__(512, 2) k_geometry(const SetDesc *__restrict__
 		if (threadIdx.x == 0) s_item = queue ? atomicAdd(queue, 1u) : next;
 		__syncthreads();
 		const uint32_t it = s_item;
-		if (it >= nitems || s_flag) break;
+		if (it >= nitems || s_flag) {
+			/* a CTA stopped by a timed-out wait reports the item it had
+			 * just dequeued, which it does not build */
+			if (s_flag && threadIdx.x == 0 && it < nitems) outs[items[it].slot].status = kStatusTimeout;
+			break;
+		}
 		next = nitems;
 		const WorkItem wi = items[it];
 		const SetDesc S = sets[wi.set];
