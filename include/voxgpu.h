@@ -311,6 +311,13 @@ VP_API int vp_rle_decode(vp_ctx *ctx, const uint32_t *words, uint32_t nwords, ui
 #define VP_STATUS_OVERFLOW 1u   /* vp_chunk_result.status: output arena too small */
 #define VP_STATUS_BAD_STREAM 2u /* vp_chunk_result.status: the chunk's stream failed the check */
 #define VP_STATUS_TIMEOUT 4u    /* vp_chunk_result.status: a bounded device wait for its data ran out */
+
+/* Self-test of the bounded wait behind VP_STATUS_TIMEOUT: one CTA arms the
+ * decoded-chunk handoff's completion barrier for 16 bytes that no copy will
+ * bring, waits as a geometry CTA does (2^16 tries) and records the outcome.
+ * *status gets VP_STATUS_TIMEOUT when the wait gave up and the kernel
+ * returned; the device stays usable. */
+VP_API int vp_selftest_handoff_wait(int device, uint32_t *status);
 VP_API int vp_rebuild_noalloc(int device, void *stream, int root_bitw, const int max_bitw[3], const uint32_t *pool,
 			      uint64_t pool_words, const uint64_t *off, const uint32_t *len, const uint16_t *shadow,
 			      uint64_t shadow_len, uint32_t shadow_w, const uint8_t *make_mesh, int lod_max,

@@ -363,3 +363,13 @@ def test_pipelined_rebuilds_reusing_one_buffer_set(ctx):
         dw.rebuild_to_host_async(lod, *bufs, res, slabs=3)
     dw.outputs_wait()
     assert _same_outputs(want[2][0], want[2][1], res, bufs) is None
+
+
+def test_handoff_wait_gives_up_and_device_stays_usable(ctx):
+    """The decoded-chunk handoff's bounded wait, armed for bytes that no
+    copy brings, gives up and reports VP_STATUS_TIMEOUT; the context then
+    rebuilds a world bit-exact."""
+    assert gpu.selftest_handoff_wait(0) == gpu.VP_STATUS_TIMEOUT
+    w = worlds.cave_world(4, (1, 1, 1), seed=2)
+    dw = gpu.DeviceWorld(ctx, w)
+    assert worlds.compare_world(dw, OracleWorld(w), None, 4) == []

@@ -189,6 +189,7 @@ def load(build_if_missing=True):
         "vp_batch_read_vbo": (I, [V, U64, U64, V]),
         "vp_batch_read_ibo": (I, [V, U64, U64, V]),
         "vp_batch_kernel_ms": (I, [V, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(U32)]),
+        "vp_selftest_handoff_wait": (I, [I, ctypes.POINTER(U32)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -674,3 +675,16 @@ class DeviceBatch:
         n = ctypes.c_uint32()
         check(self.lib.vp_batch_kernel_ms(self.h, ctypes.byref(ms), ctypes.byref(n)), "vp_batch_kernel_ms")
         return ms.value, n.value
+
+
+VP_STATUS_TIMEOUT = 4  # a bounded device wait for a chunk's data ran out
+
+
+def selftest_handoff_wait(device=0):
+    """Run the self-test of the decoded-chunk handoff's bounded wait on a
+    barrier armed for bytes that never come; returns the status it recorded
+    (VP_STATUS_TIMEOUT when the wait gave up and the kernel returned)."""
+    lib = load()
+    st = ctypes.c_uint32(0)
+    check(lib.vp_selftest_handoff_wait(device, ctypes.byref(st)), "vp_selftest_handoff_wait")
+    return st.value
