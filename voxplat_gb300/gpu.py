@@ -3,8 +3,10 @@
 `Context` and `DeviceWorld` mirror the C ABI one to one; `rebuild_world`
 is the convenience path used by tests and the benchmark.
 """
+import atexit as _atexit
 import ctypes
 import os
+import weakref as _weakref
 
 import numpy as np
 
@@ -104,6 +106,21 @@ def make_edits(rows, arrival=None):
     return e
 
 _lib = None
+
+# Live handles, so that the interpreter's exit closes servers, worlds and
+# batches before the contexts they use (finalisation would otherwise call
+# the destructors in any order).
+_live = {k: _weakref.WeakSet() for k in ("server", "world", "batch", "ctx")}
+
+
+@_atexit.register
+def _close_all():
+    for kind in ("server", "world", "batch", "ctx"):
+        for obj in list(_live[kind]):
+            try:
+                obj.close()
+            except Exception:
+                pass
 
 
 def lib_path():
@@ -216,6 +233,7 @@ class Context:
         h = ctypes.c_void_p()
         check(self.lib.vp_ctx_create(device, ctypes.byref(h)), "vp_ctx_create")
         self.h = h
+        _live["ctx"].add(self)
 
     def close(self):
         if self.h:
@@ -274,6 +292,7 @@ class DeviceWorld:
         mb = (ctypes.c_int * 3)(*self.max_bitw)
         check(self.lib.vp_world_create(ctx.h, root_bitw, mb, ctypes.byref(h)), "vp_world_create")
         self.h = h
+        _live["world"].add(self)
         if world is not None:
             self.upload(world)
 
@@ -293,6 +312,7 @@ class DeviceWorld:
             hdr = np.frombuffer(f.read(24), np.int32)
         dw = cls.__new__(cls)
         dw.ctx, dw.lib, dw.world, dw.h = ctx, ctx.lib, None, h
+        _live["world"].add(dw)
         dw.root_bitw, dw.max_bitw = int(hdr[2]), tuple(int(b) for b in hdr[3:6])
         dw.nchunks = 1 << sum(dw.max_bitw)
         return dw
@@ -528,6 +548,7 @@ class EditServer:
         h = ctypes.c_void_p()
         check(self.lib.vp_server_create(world.h, ctypes.byref(cfg), ctypes.byref(h)), "vp_server_create")
         self.h = h
+        _live["server"].add(self)
 
     def close(self):
         if self.h:
@@ -580,6 +601,7 @@ class DeviceBatch:
         h = ctypes.c_void_p()
         check(self.lib.vp_batch_create(ctx.h, self.n, _p(rb), ctypes.byref(h)), "vp_batch_create")
         self.h = h
+        _live["batch"].add(self)
         lens = np.array([int(w.len[0]) for w in chunk_worlds], np.uint32)
         offs = np.zeros(self.n, np.uint64)
         pieces, o = [], 0
