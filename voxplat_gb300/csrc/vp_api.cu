@@ -821,7 +821,7 @@ static int enqueue_group(vp_world *w, int lod_max, uint64_t svl_cap_units)
 	a.out_cap = (uint64_t)w->garena_units * 8u;
 	cudaError_t e = launch_group(w->d_outs, w->nchunks, lod_max, a, st);
 	if (e != cudaSuccess) return cuda_fail(e, "group launch");
-	w->launches += 3;
+	w->launches += lod_max >= 1 ? 4 : 1; /* level 0, then scatter, scan and copy */
 	w->grouped_lod = lod_max;
 	return VP_OK;
 }
@@ -917,7 +917,7 @@ static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 		Lg.n_items = w->n_geo;
 		e = launch_geometry(w->root_bitw, Lg, st);
 		if (e != cudaSuccess) return cuda_fail(e, "geometry launch");
-		w->launches += 2;
+		w->launches += 2 + (L.n_uni ? 1 : 0); /* shell, single-run shells, geometry */
 	}
 	if (ctx->timing) cudaEventRecord(e2, st);
 	w->grouped_lod = -1;
@@ -1363,7 +1363,9 @@ static int stream_rebuild(vp_world *w, int lod_max, unsigned flags, int slabs, v
 		CK(cudaGetLastError());
 		CK(cudaEventRecord(w->slab_ev[k], st));
 	}
-	w->launches += 1 + slabs;
+	/* cursors, shell, single-run shells, and per slab geometry and the
+	 * cursor snapshot */
+	w->launches += 2 + (L.n_uni ? 1 : 0) + 2 * slabs;
 	w->grouped_lod = -1;
 	if ((flags & VP_REBUILD_GROUP) && (rc = enqueue_group(w, lod_max, limit[0]))) return rc;
 	w->last_lod = lod_max;
