@@ -724,7 +724,6 @@ struct BigAcc {
 	const uint32_t *__restrict__ stream;
 	const BigMem &m;
 	__device__ __forceinline__ uint32_t occ(int x, int y, int z) const { return occ_at_big(m, x, y, z); }
-	__device__ __forceinline__ uint32_t colour(int x, int y, int z) const { return colour_at_big(stream, m, x, y, z); }
 	__device__ __forceinline__ uint32_t mcolour(int x, int y, int z) const
 	{
 		return mask_colour_big(S, stream, m, x, y, z);

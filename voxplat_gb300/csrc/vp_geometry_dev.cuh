@@ -827,7 +827,6 @@ struct SmallAcc {
 	const uint32_t *__restrict__ stream;
 	const Smem &m;
 	__device__ __forceinline__ uint32_t occ(int x, int y, int z) const { return occ_at<RB>(m, x, y, z); }
-	__device__ __forceinline__ uint32_t colour(int x, int y, int z) const { return colour_at<RB>(stream, m, x, y, z); }
 	__device__ __forceinline__ uint32_t mcolour(int x, int y, int z) const
 	{
 		return mask_colour<RB>(S, stream, m, x, y, z);
@@ -844,7 +843,9 @@ __device__ __forceinline__ void emit_face(const Acc &A, const SetDesc &S, const 
 {
 	const int nx = x + (i == 0), ny = y + (i == 1), nz = z + (i == 2);
 	const uint32_t a_solid = A.occ(x, y, z);
-	const uint32_t colour = a_solid ? A.colour(x, y, z) : A.mcolour(nx, ny, nz);
+	/* the solid voxel's colour: A's (inside the chunk), or B's (possibly
+	 * on a + boundary plane, from the neighbour's shell): one lookup path */
+	const uint32_t colour = a_solid ? A.mcolour(x, y, z) : A.mcolour(nx, ny, nz);
 	const int normal = a_solid ? 0 : 1;
 	const int ax = a_solid ? nx : x, ay = a_solid ? ny : y, az = a_solid ? nz : z;
 	const int bx = a_solid ? x : nx, by = a_solid ? y : ny, bz = a_solid ? z : nz;
@@ -869,21 +870,26 @@ __device__ __forceinline__ void emit_face(const Acc &A, const SetDesc &S, const 
 	uint32_t wsx = (cv[0] << RB) + (uint32_t)bx;
 	uint32_t wsy = (cv[1] << RB) + (uint32_t)by;
 	uint32_t wsz = (cv[2] << RB) + (uint32_t)bz;
-	uint32_t shadow = 0;
-	if (i == 0 && normal)
-		shadow = shadow_sample_normal(S, wsx, wsy, wsz);
-	else if (i == 1 && !normal)
-		shadow = shadow_sample(S, wsx, wsy, wsz);
+	/* The shadow samples, one path for every lane (uint32 index arithmetic
+	 * as shadow_sample / shadow_sample_normal, src/chunkset/shadow.h:45-75):
+	 * the three map entries around b are read, then combined per case.
+	 *   i = 0, B air:   shadow_sample_normal(ws): b, b - 1, lim = wsy + 1
+	 *   i = 1, A air:   shadow_sample(ws):        b, b + 1, lim = wsy + 1
+	 *   i = 2 (diamond, z = wsz - normal + 1 when B is air):
+	 *                   !shadow_sample(wsx, wsy, z):     b, b + 1, lim = wsy + 1
+	 *                   !shadow_sample(wsx, wsy - 1, z): b - 1, b, lim = wsy
+	 * A lim of 0 reads as shadowed, as the reference's early return. */
+	const uint32_t zq = i == 2 ? wsz - (uint32_t)normal + (a_solid ? 1u : 0u) : wsz;
+	const uint32_t b = (wsx + wsy) + S.shadow_w * zq;
+	const uint32_t vm = shadow_at(S, b - 1u), v0 = shadow_at(S, b), vp = shadow_at(S, b + 1u);
+	const uint32_t lim = wsy + 1u;
+	uint32_t shadow = 0, diamond = 3;
+	if (i == 0 && normal) shadow = !((v0 < lim) & (vm < lim));
+	if (i == 1 && !normal) shadow = !((v0 < lim) & (vp < lim));
+	if (i == 2) diamond = ((uint32_t)((v0 < lim) & (vp < lim)) << 1) | (uint32_t)((vm < wsy) & (v0 < wsy));
 	if (i == 0) wsx -= (uint32_t)normal;
 	else if (i == 1) wsy -= (uint32_t)normal;
 	else wsz -= (uint32_t)normal;
-	uint32_t diamond = 3;
-	if (i == 2) {
-		shadow = 0;
-		const uint32_t sz = wsz + (a_solid ? 1u : 0u); /* +1 when B is air */
-		diamond = (uint32_t)(!shadow_sample(S, wsx, wsy, sz)) << 1;
-		diamond |= (uint32_t)(!shadow_sample(S, wsx, wsy - 1u, sz));
-	}
 	const uint32_t qo = quad_offsets(i);
 	const uint32_t word0 = colour | ((uint32_t)(i + 3 * normal) << 8) | (shadow << 13) | (diamond << 14);
 	uint32_t out[8];
