@@ -724,15 +724,20 @@ def draw_cull(dw, reps=20):
 
 def render_frame(dw, modes_eye, width=1920, height=1080, reps=5):
     """Draw cull + CUDA rasteriser of the splat and mesh shaders at 1080p
-    from the bench camera, through the C ABI (frame back to host)."""
+    from the bench camera, through the C ABI (frame back to host, into
+    page-locked RGBA and depth arrays reused from frame to frame)."""
+    import torch
     from voxplat_gb300.camera import camera
     eye = np.asarray(modes_eye, np.float32)
     cam = camera(eye, eye + np.array([0.6, -0.25, 1.0]), width, height, fov_deg=70.0, far=4096.0)
     mq, sq = dw.cull(cam["view_projection"], eye)
-    rgba, depth, stats = dw.render(cam, mq, sq)
+    host_rgba = torch.empty((height, width), dtype=torch.int32).pin_memory()
+    host_depth = torch.empty((height, width), dtype=torch.float32).pin_memory()
+    out = (host_rgba.numpy().view(np.uint32), host_depth.numpy())
+    rgba, depth, stats = dw.render(cam, mq, sq, out=out)
     t0 = time.perf_counter()
     for _ in range(reps):
-        rgba, depth, stats = dw.render(cam, mq, sq)
+        rgba, depth, stats = dw.render(cam, mq, sq, out=out)
     ms = (time.perf_counter() - t0) / reps * 1e3
     return {"width": width, "height": height, "ms_per_frame": round(ms, 3), "splats": int(stats[0]),
             "triangles": int(stats[1]), "pixels_drawn": int((depth < 1.0).sum()),

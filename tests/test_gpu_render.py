@@ -60,3 +60,31 @@ def test_frames_match_oracle(ctx, k):
     assert drawn > 500, drawn
     assert np.array_equal(rgba, f.rgba), int((rgba != f.rgba).sum())
     assert np.array_equal(depth.view(np.uint32), f.depth.view(np.uint32))
+
+
+def test_frame_into_caller_arrays(ctx):
+    """render(out=...) writes the same frame into the caller's arrays (here
+    page-locked, reused for a second frame) and rejects mismatched ones."""
+    import torch
+    w = worlds.cave_world(5, (2, 1, 2), seed=19)
+    dw = gpu.DeviceWorld(ctx, w)
+    eye, target, fov = CAMS[0]
+    eye = np.array(eye, np.float32)
+    dw.camera_modes(eye)
+    dw.rebuild(lod_max=4, group=True)
+    dw.finish()
+    cam = camera(eye, target, 320, 200, fov_deg=fov, far=4096.0)
+    mq, sq = dw.cull(cam["view_projection"], eye)
+    want_rgba, want_depth, want_stats = dw.render(cam, mq, sq)
+    host_rgba = torch.empty((200, 320), dtype=torch.int32).pin_memory()
+    host_depth = torch.empty((200, 320), dtype=torch.float32).pin_memory()
+    out = (host_rgba.numpy().view(np.uint32), host_depth.numpy())
+    for _ in range(2):
+        rgba, depth, stats = dw.render(cam, mq, sq, out=out)
+        assert rgba is out[0] and depth is out[1]
+        assert np.array_equal(rgba, want_rgba)
+        assert np.array_equal(depth.view(np.uint32), want_depth.view(np.uint32))
+        assert np.array_equal(stats, want_stats)
+    with pytest.raises(ValueError):
+        dw.render(cam, mq, sq, out=(np.zeros((200, 321), np.uint32), np.zeros((200, 320), np.float32)))
+    dw.close()

@@ -1182,7 +1182,8 @@ VP_API int vp_world_render(vp_world *w, const vp_camera *cam, const uint32_t *me
 	CK(cudaStreamSynchronize(st));
 	/* frame words, RGBA, depth, and the two lists of large footprints */
 	const uint32_t big_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(totals[0] + totals[1], 1), 4u << 20);
-	const size_t f_rgba = a256(8u * npx), f_depth = a256(f_rgba + 4u * npx), f_big = a256(f_depth + 4u * npx);
+	const size_t f_rgba = a256(8u * npx), f_depth = a256(f_rgba + 4u * npx), f_raya = a256(f_depth + 4u * npx);
+	const size_t f_rayb = a256(f_raya + 16u * npx), f_big = a256(f_rayb + 8u * npx);
 	const size_t frame_bytes = a256(f_big + 16u * (size_t)big_cap);
 	if (w->frame_cap < frame_bytes) {
 		dev_free(w->d_frame);
@@ -1197,6 +1198,9 @@ VP_API int vp_world_render(vp_world *w, const vp_camera *cam, const uint32_t *me
 	a.light[0] = -1.0f / llen;
 	a.light[1] = 1.0f / llen;
 	a.light[2] = 0.0f / llen;
+	/* one IEEE single-precision division (both hosts evaluate float
+	 * expressions in float), the value every fragment computed before */
+	a.fog_start = 256.0f / cam->far_plane;
 	a.splats = w->d_garena;
 	a.splats_l0 = (const int16_t *)w->d_arena[0];
 	a.segs = (const RenderSeg *)(R + o_seg);
@@ -1210,6 +1214,8 @@ VP_API int vp_world_render(vp_world *w, const vp_camera *cam, const uint32_t *me
 	a.nmesh = n_mesh;
 	a.ntris = totals[1];
 	a.frame = (unsigned long long *)w->d_frame;
+	a.ray_a = (float4 *)(w->d_frame + f_raya);
+	a.ray_b = (float2 *)(w->d_frame + f_rayb);
 	a.big = (uint64_t *)(w->d_frame + f_big);
 	a.big_count = (uint32_t *)(R + o_bc);
 	a.big_cap = big_cap;

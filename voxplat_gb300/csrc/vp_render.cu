@@ -55,21 +55,37 @@ __device__ __forceinline__ void frame_put(unsigned long long *frame, int width, 
 	atomicMin(frame + (size_t)py * width + px, v);
 }
 
-__device__ __forceinline__ void fog_mix(const float col[3], float depth, float far_plane, float out[3])
+/* fog_start = 256 / far, rounded once per frame on the host */
+__device__ __forceinline__ void fog_mix(const float col[3], float depth, float fog_start, float out[3])
 {
-	const float fog_start = __fdiv_rn(256.0f, far_plane);
 	const float fog = __fsqrt_rn(fmaxf(__fsub_rn(depth, fog_start), 0.0001f));
 	const float fc[3] = {0.5f, 0.5f, 0.7f};
 	for (int i = 0; i < 3; i++) out[i] = __fadd_rn(__fmul_rn(col[i], __fsub_rn(1.0f, fog)), __fmul_rn(fc[i], fog));
 }
 
-__global__ void k_frame_clear(unsigned long long *frame, uint64_t n)
+/* Clears the frame and fills the per-pixel ray table: the ray through the
+ * pixel's centre (splat.frag.glsl's ray from the inverse projection and
+ * rotation, normalised) and its reciprocals, the same for every splat. */
+__global__ void k_frame_clear(RenderArgs a, uint64_t n)
 {
 	const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
 	if (i >= n) return;
 	const float bg[3] = {0.5f, 0.5f, 0.7f};
 	const uint32_t rgba = to8(bg[0]) | (to8(bg[1]) << 8) | (to8(bg[2]) << 16) | (255u << 24);
-	frame[i] = ((unsigned long long)__float_as_uint(1.0f) << 32) | rgba;
+	a.frame[i] = ((unsigned long long)__float_as_uint(1.0f) << 32) | rgba;
+	const int px = (int)(i % (uint64_t)a.cam.width), py = (int)(i / (uint64_t)a.cam.width);
+	const float W = __int2float_rn(a.cam.width), H = __int2float_rn(a.cam.height);
+	const float rc[4] = {__fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn(__int2float_rn(px), 0.5f), W), 2.0f), 1.0f),
+			     __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn(__int2float_rn(py), 0.5f), H), 2.0f), 1.0f), -1.0f,
+			     1.0f};
+	float r4[4];
+	mat_vec(a.cam.inv_proj_view_rot, rc, r4);
+	const float rv[3] = {__fdiv_rn(r4[0], r4[3]), __fdiv_rn(r4[1], r4[3]), __fdiv_rn(r4[2], r4[3])};
+	const float len =
+		__fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(rv[0], rv[0]), __fmul_rn(rv[1], rv[1])), __fmul_rn(rv[2], rv[2])));
+	const float ray[3] = {__fdiv_rn(rv[0], len), __fdiv_rn(rv[1], len), __fdiv_rn(rv[2], len)};
+	a.ray_a[i] = make_float4(ray[0], ray[1], ray[2], __fdiv_rn(1.0f, ray[0]));
+	a.ray_b[i] = make_float2(__fdiv_rn(1.0f, ray[1]), __fdiv_rn(1.0f, ray[2]));
 }
 
 /* ---------------- splats ---------------- */
@@ -115,21 +131,14 @@ __device__ bool splat_setup(const RenderArgs &a, const int16_t *sp, float lod, S
 
 __device__ void splat_fragment(const RenderArgs &a, const SplatSetup &s, int px, int py)
 {
-	const float W = __int2float_rn(a.cam.width), H = __int2float_rn(a.cam.height);
-	const float rc[4] = {__fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn(__int2float_rn(px), 0.5f), W), 2.0f), 1.0f),
-			     __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn(__int2float_rn(py), 0.5f), H), 2.0f), 1.0f), -1.0f,
-			     1.0f};
-	float r4[4];
-	mat_vec(a.cam.inv_proj_view_rot, rc, r4);
-	const float rv[3] = {__fdiv_rn(r4[0], r4[3]), __fdiv_rn(r4[1], r4[3]), __fdiv_rn(r4[2], r4[3])};
-	const float len =
-		__fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(rv[0], rv[0]), __fmul_rn(rv[1], rv[1])), __fmul_rn(rv[2], rv[2])));
-	const float ray[3] = {__fdiv_rn(rv[0], len), __fdiv_rn(rv[1], len), __fdiv_rn(rv[2], len)};
+	const size_t p = (size_t)py * a.cam.width + px;
+	const float4 ra = a.ray_a[p];
+	const float2 rb = a.ray_b[p];
+	const float ray[3] = {ra.x, ra.y, ra.z}, inv[3] = {ra.w, rb.x, rb.y};
 	const float hl = __fmul_rn(0.5f, s.lod);
 	float tmin[3], tmax[3];
 	for (int i = 0; i < 3; i++) {
-		const float inv = __fdiv_rn(1.0f, ray[i]);
-		const float tb = __fmul_rn(__fsub_rn(s.vv[i], hl), inv), tt = __fmul_rn(__fadd_rn(s.vv[i], hl), inv);
+		const float tb = __fmul_rn(__fsub_rn(s.vv[i], hl), inv[i]), tt = __fmul_rn(__fadd_rn(s.vv[i], hl), inv[i]);
 		tmin[i] = fminf(tt, tb);
 		tmax[i] = fmaxf(tt, tb);
 	}
@@ -151,7 +160,7 @@ __device__ void splat_fragment(const RenderArgs &a, const SplatSetup &s, int px,
 	const float g = fmaxf(fmaxf(0.7f, s.shadow), s_);
 	const float col[3] = {__fmul_rn(s.vcol[0], g), __fmul_rn(s.vcol[1], g), __fmul_rn(s.vcol[2], g)};
 	float out[3];
-	fog_mix(col, depth, a.cam.far_plane, out);
+	fog_mix(col, depth, a.fog_start, out);
 	frame_put(a.frame, a.cam.width, px, py, depth, out);
 }
 
@@ -207,16 +216,26 @@ struct MeshVert {
 	int diamond;
 };
 
-__device__ bool mesh_vertex(const RenderArgs &a, const int16_t *v, MeshVert &o)
+/* The vertex stage in two parts: the window position, which decides
+ * whether the triangle is drawn at all, and the varyings, computed only for
+ * triangles that are. */
+__device__ bool mesh_vertex_pos(const RenderArgs &a, const int16_t *v, MeshVert &o)
 {
 	const float a4[4] = {__int2float_rn(v[0]), __int2float_rn(v[1]), __int2float_rn(v[2]), 1.0f};
-	float clip[4], vt[4];
+	float clip[4];
 	mat_vec(a.cam.view_projection, a4, clip);
-	mat_vec(a.cam.view_translation, a4, vt);
 	o.w = clip[3];
 	const float W = __int2float_rn(a.cam.width), H = __int2float_rn(a.cam.height);
 	o.xw = __fmul_rn(__fadd_rn(__fmul_rn(__fdiv_rn(clip[0], clip[3]), 0.5f), 0.5f), W);
 	o.yw = __fmul_rn(__fadd_rn(__fmul_rn(__fdiv_rn(clip[1], clip[3]), 0.5f), 0.5f), H);
+	return clip[3] > 0.0f;
+}
+
+__device__ void mesh_vertex_attr(const RenderArgs &a, const int16_t *v, MeshVert &o)
+{
+	const float a4[4] = {__int2float_rn(v[0]), __int2float_rn(v[1]), __int2float_rn(v[2]), 1.0f};
+	float vt[4];
+	mat_vec(a.cam.view_translation, a4, vt);
 	const float d = __fsqrt_rn(__fadd_rn(
 		__fadd_rn(__fadd_rn(__fmul_rn(vt[0], vt[0]), __fmul_rn(vt[1], vt[1])), __fmul_rn(vt[2], vt[2])),
 		__fmul_rn(vt[3], vt[3])));
@@ -238,7 +257,6 @@ __device__ bool mesh_vertex(const RenderArgs &a, const int16_t *v, MeshVert &o)
 	o.uv[0] = (ui == 1 || ui == 2) ? 1.0f : 0.0f;
 	o.uv[1] = ui >= 2 ? 1.0f : 0.0f;
 	o.diamond = (c >> 14) & 3;
-	return clip[3] > 0.0f;
 }
 
 __device__ __forceinline__ float edge_fn(float ax, float ay, float bx, float by, float px, float py)
@@ -272,9 +290,11 @@ __device__ bool tri_setup(const RenderArgs &a, uint64_t t, TriSetup &s)
 	const uint64_t local = t - a.mesh_first[lo];
 	const uint32_t *ib = a.ibo + m.ibo_off + local * 3u;
 	const int16_t *vb = a.vbo + m.vbo_off;
-	bool ok = true;
-	for (int k = 0; k < 3; k++) ok &= mesh_vertex(a, vb + 4u * (size_t)ib[k], s.v[k]);
-	if (!ok) return false;
+	const int16_t *vp[3];
+	for (int k = 0; k < 3; k++) {
+		vp[k] = vb + 4u * (size_t)ib[k];
+		if (!mesh_vertex_pos(a, vp[k], s.v[k])) return false;
+	}
 	s.area = edge_fn(s.v[0].xw, s.v[0].yw, s.v[1].xw, s.v[1].yw, s.v[2].xw, s.v[2].yw);
 	if (!(s.area > 0.0f)) return false;
 	const float mnx = fminf(fminf(s.v[0].xw, s.v[1].xw), s.v[2].xw), mxx = fmaxf(fmaxf(s.v[0].xw, s.v[1].xw), s.v[2].xw);
@@ -287,19 +307,30 @@ __device__ bool tri_setup(const RenderArgs &a, uint64_t t, TriSetup &s)
 	s.tl[0] = top_left(s.v[1].xw, s.v[1].yw, s.v[2].xw, s.v[2].yw);
 	s.tl[1] = top_left(s.v[2].xw, s.v[2].yw, s.v[0].xw, s.v[0].yw);
 	s.tl[2] = top_left(s.v[0].xw, s.v[0].yw, s.v[1].xw, s.v[1].yw);
-	return s.x0 <= s.x1 && s.y0 <= s.y1;
+	if (!(s.x0 <= s.x1 && s.y0 <= s.y1)) return false;
+	for (int k = 0; k < 3; k++) mesh_vertex_attr(a, vp[k], s.v[k]);
+	return true;
+}
+
+/* Whether the pixel centre (px, py) is inside the triangle (top-left rule
+ * on edges), and its three edge values. */
+__device__ __forceinline__ bool tri_inside(const TriSetup &s, int px, int py, float e[3])
+{
+	const MeshVert *v = s.v;
+	const float fx = __fadd_rn(__int2float_rn(px), 0.5f), fy = __fadd_rn(__int2float_rn(py), 0.5f);
+	e[0] = edge_fn(v[1].xw, v[1].yw, v[2].xw, v[2].yw, fx, fy);
+	e[1] = edge_fn(v[2].xw, v[2].yw, v[0].xw, v[0].yw, fx, fy);
+	e[2] = edge_fn(v[0].xw, v[0].yw, v[1].xw, v[1].yw, fx, fy);
+	return (e[0] > 0.0f || (e[0] == 0.0f && s.tl[0])) && (e[1] > 0.0f || (e[1] == 0.0f && s.tl[1])) &&
+	       (e[2] > 0.0f || (e[2] == 0.0f && s.tl[2]));
 }
 
 __device__ void tri_fragment(const RenderArgs &a, const TriSetup &s, int px, int py)
 {
 	const MeshVert *v = s.v;
-	const float fx = __fadd_rn(__int2float_rn(px), 0.5f), fy = __fadd_rn(__int2float_rn(py), 0.5f);
-	const float e0 = edge_fn(v[1].xw, v[1].yw, v[2].xw, v[2].yw, fx, fy);
-	const float e1 = edge_fn(v[2].xw, v[2].yw, v[0].xw, v[0].yw, fx, fy);
-	const float e2 = edge_fn(v[0].xw, v[0].yw, v[1].xw, v[1].yw, fx, fy);
-	if (!(e0 > 0.0f || (e0 == 0.0f && s.tl[0])) || !(e1 > 0.0f || (e1 == 0.0f && s.tl[1])) ||
-	    !(e2 > 0.0f || (e2 == 0.0f && s.tl[2])))
-		return;
+	float e[3];
+	if (!tri_inside(s, px, py, e)) return;
+	const float e0 = e[0], e1 = e[1], e2 = e[2];
 	const float q0 = __fdiv_rn(__fdiv_rn(e0, s.area), v[0].w);
 	const float q1 = __fdiv_rn(__fdiv_rn(e1, s.area), v[1].w);
 	const float q2 = __fdiv_rn(__fdiv_rn(e2, s.area), v[2].w);
@@ -321,7 +352,7 @@ __device__ void tri_fragment(const RenderArgs &a, const TriSetup &s, int px, int
 	if (nrm[1] < -0.9f || nrm[0] > 0.9f)
 		for (int i = 0; i < 3; i++) c2[i] = __fmul_rn(col[i], 0.6f);
 	float out[3];
-	fog_mix(c2, depth, a.cam.far_plane, out);
+	fog_mix(c2, depth, a.fog_start, out);
 	frame_put(a.frame, a.cam.width, px, py, depth, out);
 }
 
@@ -366,7 +397,7 @@ __global__ void k_frame_resolve(const unsigned long long *frame, uint64_t n, uin
 cudaError_t launch_render(const RenderArgs &a, uint32_t *rgba, float *depth, int sm_count, cudaStream_t st)
 {
 	const uint64_t npx = (uint64_t)a.cam.width * a.cam.height;
-	k_frame_clear<<<(unsigned)((npx + 255) / 256), 256, 0, st>>>(a.frame, npx);
+	k_frame_clear<<<(unsigned)((npx + 255) / 256), 256, 0, st>>>(a, npx);
 	cudaError_t e = cudaMemsetAsync(a.big_count, 0, 2 * sizeof(uint32_t), st);
 	if (e != cudaSuccess) return e;
 	if (a.ntris) {

@@ -28,6 +28,7 @@ struct RenderMesh {
 struct RenderArgs {
 	RenderCam cam;
 	float light[3];                 /* normalize(-1, 1, 0) */
+	float fog_start;                /* 256 / far_plane (mesh.frag.glsl, splat.frag.glsl fog) */
 	const int16_t *splats;     /* grouped lists of LOD >= 1 nodes */
 	const int16_t *splats_l0;  /* the splat arena: LOD 0 nodes are chunks' level-0 segments */
 	const RenderSeg *segs;
@@ -41,6 +42,10 @@ struct RenderArgs {
 	uint32_t nmesh;
 	uint64_t ntris;
 	unsigned long long *frame;      /* width x height, (depth << 32) | RGBA8 */
+	/* per pixel, from the camera alone: the splat fragments' ray direction
+	 * and its reciprocals, ray_a = (dx, dy, dz, 1/dx), ray_b = (1/dy, 1/dz) */
+	float4 *ray_a;
+	float2 *ray_b;
 	uint64_t *big;                  /* [2][big_cap]: large splats, large triangles */
 	uint32_t *big_count;            /* [2] */
 	uint32_t big_cap;

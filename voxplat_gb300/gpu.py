@@ -432,14 +432,23 @@ class DeviceWorld:
                                      len(sq), ctypes.byref(ns)), "vp_world_cull")
         return mq[:nm.value].copy(), sq[:ns.value].copy()
 
-    def render(self, cam, mesh_queue, svl_queue):
+    def render(self, cam, mesh_queue, svl_queue, out=None):
         """(rgba[h, w] uint32, depth[h, w] float32, stats[4]) of the drawn
-        queues; cam is a voxplat_gb300.camera.camera() dict."""
+        queues; cam is a voxplat_gb300.camera.camera() dict. `out` = (rgba,
+        depth) arrays of those shapes and types to write the frame into
+        (page-locked ones make the copy back a direct one)."""
         c = Camera.from_dict(cam)
         mq = np.ascontiguousarray(mesh_queue, np.uint32)
         sq = np.ascontiguousarray(svl_queue, np.uint32)
-        rgba = np.zeros((cam["height"], cam["width"]), np.uint32)
-        depth = np.zeros((cam["height"], cam["width"]), np.float32)
+        shape = (cam["height"], cam["width"])
+        if out is None:
+            rgba = np.zeros(shape, np.uint32)
+            depth = np.zeros(shape, np.float32)
+        else:
+            rgba, depth = out
+            if (rgba.shape != shape or rgba.dtype != np.uint32 or not rgba.flags.c_contiguous or
+                    depth.shape != shape or depth.dtype != np.float32 or not depth.flags.c_contiguous):
+                raise ValueError("render: out must be C-contiguous uint32 and float32 arrays of shape %r" % (shape,))
         stats = np.zeros(4, np.uint64)
         check(self.lib.vp_world_render(self.h, ctypes.byref(c), _p(mq), len(mq), _p(sq), len(sq), _p(rgba),
                                        _p(depth), _p(stats)), "vp_world_render")
