@@ -284,6 +284,15 @@ def cpu_baseline(world, modes, budget_s=12.0, threads=None, check=None):
     dt = time.perf_counter() - t0
     out = {"value": round(n / dt, 1), "unit": "chunks/s", "cores": threads, "kind": "port",
            "sample": "%d of the %d chunks (random, seed 1), cold decode, same modes/LOD" % (n, world.nchunks)}
+    # the per-chunk pipeline on one core (the reference's single-thread view),
+    # on a sample sized from the parallel rate for about two seconds
+    n1 = int(min(world.nchunks, max(32, 2.0 * out["value"] / threads)))
+    t0 = time.perf_counter()
+    o.rebuild(order[:n1], modes, LOD_MAX, 1)
+    dt1 = time.perf_counter() - t0
+    out["single_thread"] = {"value": round(n1 / dt1, 1), "unit": "chunks/s", "cores": 1,
+                            "voxels_per_s": round(n1 / dt1 * world.R ** 3, 1),
+                            "sample": "the first %d chunks of the same sample" % n1}
     cal = port_calibration()
     if cal:
         out["calibration"] = cal
