@@ -84,7 +84,7 @@ struct Geo {
 struct Smem {
 	uint64_t *occ, *rs, *lv;
 	uint32_t *rank, *tmp;
-	uint32_t *grp;   /* emission base of every 32-row group */
+	uint32_t *grp;   /* emission base of every emission group (32 or 64 rows) */
 	uint16_t *glist; /* the groups with any output, in order */
 	uint64_t *e0p;   /* splat mode: L0 mask rows of the x = R, y = R, z = R planes */
 	uint64_t *sv;    /* splat mode: two saved occupancy planes */
@@ -650,7 +650,7 @@ __device__ void splat_prepare(const Smem &m)
 }
 
 /* Per chunk size 2^RB and LOD level l: the word offset of the level's rows
- * in the level-row area, its first 32-row emission group, and the
+ * in the level-row area, its first emission group, and the
  * multiply-shift constant that divides a row index by n = (R >> l) + 1
  * (q = umulhi(r, magic) equals r / n for every r < 2^17 and n <= 129). */
 struct LevelTab {
@@ -658,6 +658,11 @@ struct LevelTab {
 	int gstart[8][kMaxLevels + 1];
 	uint32_t magic[8][kMaxLevels];
 };
+
+/* Rows per emission group of level l: 32, one per lane, except level 0 of
+ * chunks up to 64^3, whose groups are 64 rows, two consecutive rows per
+ * lane (half the groups to set up, and fewer partly filled steps). */
+constexpr int group_rows(int rb, int l) { return (l == 0 && rb <= 6) ? 64 : 32; }
 
 constexpr LevelTab make_level_tab()
 {
@@ -670,7 +675,7 @@ constexpr LevelTab make_level_tab()
 			t.off[rb][l] = l == 0 ? 0 : off;
 			if (l >= 1) off += n * n;
 			t.gstart[rb][l] = g;
-			g += (n * n + 31) / 32;
+			g += (n * n + group_rows(rb, l) - 1) / group_rows(rb, l);
 			t.magic[rb][l] = n == 1 ? 0u : (uint32_t)(0xFFFFFFFFu / (uint32_t)n + 1u);
 		}
 		t.gstart[rb][kMaxLevels] = g;
@@ -1209,7 +1214,7 @@ __device__ __forceinline__ bool shadow_window_inside(const SetDesc &S, const uin
 
 static_assert(kMaxLevels == 8, "the level switches have one case per level");
 
-/* Level of 32-row emission group g. */
+/* Level of emission group g. */
 template <int RB>
 __device__ __forceinline__ int group_level(int g)
 {
@@ -1256,36 +1261,39 @@ __device__ __forceinline__ void build_level(const Smem &m)
 	}
 }
 
-/* Cells of 32-row group g of level L (all lanes call; every lane gets it).
- * Used for level 0, whose rows come from several sources; build_level
- * counts the groups of the levels above as it writes their rows. */
+/* Cells of group g of level L (all lanes call; every lane gets it). Used
+ * for level 0, whose rows come from several sources; build_level counts
+ * the groups of the levels above as it writes their rows. */
 template <int RB, int L>
 __device__ __forceinline__ uint32_t count_group(const Smem &m, int g)
 {
 	constexpr int R = Geo<RB>::R;
 	constexpr uint32_t n = (uint32_t)(R >> L) + 1u;
-	const uint32_t r = (uint32_t)(g - c_lv.gstart[RB][L]) * 32u + (threadIdx.x & 31u);
+	constexpr uint32_t rows = (uint32_t)group_rows(RB, L), per_lane = rows / 32u;
+	const uint32_t r0 = (uint32_t)(g - c_lv.gstart[RB][L]) * rows + (threadIdx.x & 31u) * per_lane;
 	uint32_t c = 0;
-	if (r < n * n) {
-		const uint32_t z = r / n, y = r - z * n;
-		uint32_t xr;
-		c = __popcll(level_row<RB>(m, L, (int)y, (int)z, xr)) + xr;
+#pragma unroll
+	for (uint32_t i = 0; i < per_lane; i++) {
+		const uint32_t r = r0 + i;
+		if (r < n * n) {
+			const uint32_t z = r / n, y = r - z * n;
+			uint32_t xr;
+			c += __popcll(level_row<RB>(m, L, (int)y, (int)z, xr)) + xr;
+		}
 	}
 	return __reduce_add_sync(kFull, c);
 }
 
-/* Pass 2 of one non-empty 32-row group of level L: lane s holds row s and
- * its exclusive item offset; items go one per lane per step (two per step,
- * both searches first, measured 4 % slower: more registers live across the
- * loads). Specialised per level, so the row division, the walk down and
- * the shifts are compile-time. Level 0 (three quarters of the splats) is
- * software-pipelined: a step's colour and shadow loads are issued, and
- * consumed one step later, after the next step's search and select. The
- * levels above keep the plain loop: their walk down needs the registers. */
+/* Pass 2 of one non-empty 32-row group of level L >= 1: lane s holds row s
+ * and its exclusive item offset; items go one per lane per step (two per
+ * step, both searches first, measured 4 % slower: more registers live
+ * across the loads). Specialised per level, so the row division, the walk
+ * down and the shifts are compile-time. */
 template <int RB, int L>
 __device__ __forceinline__ void splat_group(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m,
 					    const uint32_t cv[3], int g, int16_t *dst, bool sh_in)
 {
+	static_assert(L >= 1, "level 0 has splat_group_l0");
 	constexpr int R = Geo<RB>::R;
 	constexpr uint32_t n = (uint32_t)(R >> L) + 1u;
 	const int lane = threadIdx.x & 31;
@@ -1302,40 +1310,79 @@ __device__ __forceinline__ void splat_group(const SetDesc &S, const uint32_t *__
 	const uint32_t excl = inc - c;
 	const uint32_t T = __shfl_sync(kFull, inc, 31);
 	const uint32_t base = m.grp[g];
-	if (L != 0) {
-		for (uint32_t k = 0; k < T; k += 32) {
-			const uint32_t j0 = k + lane;
-			const int s0 = search_lane(excl, j0);
-			const uint32_t e0 = __shfl_sync(kFull, excl, s0), q0 = __shfl_sync(kFull, yz, s0);
-			const uint64_t w0 = shfl64(row, s0);
-			if (j0 < T) {
-				const int kk = (int)(j0 - e0);
-				const int x = kk < __popcll(w0) ? select_bit(w0, kk) : R;
-				emit_splat<RB, L>(S, stream, m, cv, x, (int)(q0 & 0xFFFFu), (int)(q0 >> 16),
-						  dst + (size_t)(base + j0) * 4, sh_in);
-			}
+	for (uint32_t k = 0; k < T; k += 32) {
+		const uint32_t j0 = k + lane;
+		const int s0 = search_lane(excl, j0);
+		const uint32_t e0 = __shfl_sync(kFull, excl, s0), q0 = __shfl_sync(kFull, yz, s0);
+		const uint64_t w0 = shfl64(row, s0);
+		if (j0 < T) {
+			const int kk = (int)(j0 - e0);
+			const int x = kk < __popcll(w0) ? select_bit(w0, kk) : R;
+			emit_splat<RB, L>(S, stream, m, cv, x, (int)(q0 & 0xFFFFu), (int)(q0 >> 16),
+					  dst + (size_t)(base + j0) * 4, sh_in);
 		}
-		return;
 	}
+}
+
+/* Pass 2 of one non-empty 64-row level-0 group (three quarters of the
+ * splats): lane s holds rows 2s and 2s + 1, consecutive in the item order,
+ * and the pair's exclusive item offset. An item's row follows from the
+ * pair's first count, its (y, z) from the row index. The loop is
+ * software-pipelined: a step's colour and shadow loads are issued, and
+ * consumed one step later, after the next step's search and select. */
+template <int RB>
+__device__ __forceinline__ void splat_group_l0(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m,
+					       const uint32_t cv[3], int g, int16_t *dst, bool sh_in)
+{
+	static_assert(group_rows(RB, 0) == 64, "level-0 groups of two rows a lane");
+	constexpr int R = Geo<RB>::R;
+	constexpr uint32_t n = (uint32_t)R + 1u;
+	const int lane = threadIdx.x & 31;
+	const uint32_t rbase = (uint32_t)(g - c_lv.gstart[RB][0]) * 64u;
+	const uint32_t r0 = rbase + 2u * (uint32_t)lane;
+	uint64_t ra = 0, rb = 0;
+	uint32_t ca = 0, cb = 0;
+	if (r0 < n * n) {
+		const uint32_t z = r0 / n, y = r0 - z * n;
+		uint32_t xr;
+		ra = e0_row<RB>(m, (int)y, (int)z, xr);
+		ca = __popcll(ra) + xr;
+	}
+	if (r0 + 1u < n * n) {
+		const uint32_t z = (r0 + 1u) / n, y = (r0 + 1u) - z * n;
+		uint32_t xr;
+		rb = e0_row<RB>(m, (int)y, (int)z, xr);
+		cb = __popcll(rb) + xr;
+	}
+	const uint32_t c = ca + cb;
+	const uint32_t inc = warp_incl_add(c);
+	const uint32_t excl = inc - c;
+	const uint32_t T = __shfl_sync(kFull, inc, 31);
+	const uint32_t base = m.grp[g];
 	SplatPend pend;
 	bool pv = false;
 	uint32_t pj = 0;
 	for (uint32_t k = 0; k < T; k += 32) {
 		const uint32_t j0 = k + lane;
 		const int s0 = search_lane(excl, j0);
-		const uint32_t e0 = __shfl_sync(kFull, excl, s0), q0 = __shfl_sync(kFull, yz, s0);
-		const uint64_t w0 = shfl64(row, s0);
+		const uint32_t e0 = __shfl_sync(kFull, excl, s0), a0 = __shfl_sync(kFull, ca, s0);
+		const uint64_t wa = shfl64(ra, s0), wb = shfl64(rb, s0);
 		const bool v = j0 < T;
-		int x = 0;
+		int x = 0, y = 0, z = 0;
 		if (v) {
-			const int kk = (int)(j0 - e0);
-			x = kk < __popcll(w0) ? select_bit(w0, kk) : R;
+			int kk = (int)(j0 - e0);
+			const bool second = kk >= (int)a0;
+			const uint64_t w = second ? wb : wa;
+			kk = second ? kk - (int)a0 : kk;
+			/* the x = R cell is its row's last item */
+			x = kk < __popcll(w) ? select_bit(w, kk) : R;
+			const uint32_t r = rbase + 2u * (uint32_t)s0 + (second ? 1u : 0u);
+			z = (int)(r / n);
+			y = (int)(r - (uint32_t)z * n);
 		}
 		/* the previous step's loads had the search and select to land */
 		if (pv) splat_finish(dst + (size_t)(base + pj) * 4, pend);
-		if (v)
-			splat_issue<RB, L>(S, stream, m, cv, x, (int)(q0 & 0xFFFFu), (int)(q0 >> 16), sh_in,
-					   dst + (size_t)(base + j0) * 4, pend);
+		if (v) splat_issue<RB, 0>(S, stream, m, cv, x, y, z, sh_in, dst + (size_t)(base + j0) * 4, pend);
 		pv = v;
 		pj = j0;
 	}
@@ -1364,7 +1411,7 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 		}
 		__syncthreads();
 	}
-	/* pass 1: splats per 32-row group; the level rows' groups were counted
+	/* pass 1: splats per group; the level rows' groups were counted
 	 * as they were built, level 0's are counted here */
 	const int ngroups = gstart[lod_max + 1];
 	for (int g = warp; g < gstart[1]; g += nw) {
@@ -1408,7 +1455,7 @@ __device__ void splat_chunk(const SetDesc &S, const uint32_t *__restrict__ strea
 		if (k >= listed) break;
 		const int g = m.glist[k];
 		switch (group_level<RB>(g)) {
-		case 0: splat_group<RB, 0>(S, stream, m, cv, g, dst, sh_in); break;
+		case 0: splat_group_l0<RB>(S, stream, m, cv, g, dst, sh_in); break;
 		case 1: splat_group<RB, 1>(S, stream, m, cv, g, dst, sh_in); break;
 		case 2: splat_group<RB, 2>(S, stream, m, cv, g, dst, sh_in); break;
 		case 3: splat_group<RB, 3>(S, stream, m, cv, g, dst, sh_in); break;
