@@ -653,10 +653,13 @@ __device__ void splat_prepare(const Smem &m)
  * in the level-row area, its first emission group, and the
  * multiply-shift constant that divides a row index by n = (R >> l) + 1
  * (q = umulhi(r, magic) equals r / n for every r < 2^17 and n <= 129). */
+constexpr int kMaxGroupsTab = 768; /* emission groups of a 128^3 chunk: 705 */
+
 struct LevelTab {
 	int off[8][kMaxLevels];
 	int gstart[8][kMaxLevels + 1];
 	uint32_t magic[8][kMaxLevels];
+	uint8_t glevel[8][kMaxGroupsTab]; /* level of each emission group */
 };
 
 /* Rows per emission group of level l: 32, one per lane, except level 0 of
@@ -679,11 +682,15 @@ constexpr LevelTab make_level_tab()
 			t.magic[rb][l] = n == 1 ? 0u : (uint32_t)(0xFFFFFFFFu / (uint32_t)n + 1u);
 		}
 		t.gstart[rb][kMaxLevels] = g;
+		for (int l = 0; l < kMaxLevels; l++)
+			for (int k = t.gstart[rb][l]; k < t.gstart[rb][l + 1] && k < kMaxGroupsTab; k++)
+				t.glevel[rb][k] = (uint8_t)l;
 	}
 	return t;
 }
 
 static __constant__ LevelTab c_lv = make_level_tab();
+static_assert(make_level_tab().gstart[7][kMaxLevels] <= kMaxGroupsTab, "group level table too short");
 
 /* (y, z) of row r of a level with n rows per z and division constant mg */
 __device__ __forceinline__ void row_yz(uint32_t r, uint32_t n, uint32_t mg, int &y, int &z)
@@ -1214,14 +1221,11 @@ __device__ __forceinline__ bool shadow_window_inside(const SetDesc &S, const uin
 
 static_assert(kMaxLevels == 8, "the level switches have one case per level");
 
-/* Level of emission group g. */
+/* Level of emission group g (one table read; warp-uniform g). */
 template <int RB>
 __device__ __forceinline__ int group_level(int g)
 {
-	int l = 0;
-#pragma unroll
-	for (int i = 1; i < kMaxLevels; i++) l += g >= c_lv.gstart[RB][i] ? 1 : 0;
-	return l;
+	return c_lv.glevel[RB][g];
 }
 
 /* Level-L rows (L >= 1): the pairwise OR of the four child rows of level
