@@ -791,6 +791,8 @@ VP_API int vp_world_reserve(vp_world *w, const uint64_t bytes[3])
 	return VP_OK;
 }
 
+static_assert(kMaxLevels == VP_MAX_LEVELS, "the node tables hold every level k_group_tables writes");
+
 static int enqueue_group(vp_world *w, int lod_max, uint64_t svl_cap_units)
 {
 	cudaStream_t st = w->ctx->stream;
@@ -807,7 +809,6 @@ static int enqueue_group(vp_world *w, int lod_max, uint64_t svl_cap_units)
 		if ((rc = dev_alloc(&w->d_garena, (size_t)w->cap[0] * 8u))) return rc;
 		w->garena_units = w->cap[0];
 	}
-	CK(cudaMemsetAsync(w->d_node_items, 0, L * n * sizeof(uint32_t), st));
 	GroupArgs a;
 	for (int i = 0; i < 3; i++) a.max_bitw[i] = (uint32_t)w->max_bitw[i];
 	a.counts = w->d_gcounts;
@@ -821,7 +822,7 @@ static int enqueue_group(vp_world *w, int lod_max, uint64_t svl_cap_units)
 	a.out_cap = (uint64_t)w->garena_units * 8u;
 	cudaError_t e = launch_group(w->d_outs, w->nchunks, lod_max, a, st);
 	if (e != cudaSuccess) return cuda_fail(e, "group launch");
-	w->launches += lod_max >= 1 ? 4 : 1; /* level 0, then scatter, scan and copy */
+	w->launches += lod_max >= 1 ? 3 : 1; /* node tables and counts, then scan and copy */
 	w->grouped_lod = lod_max;
 	return VP_OK;
 }

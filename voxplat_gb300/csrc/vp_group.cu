@@ -16,8 +16,9 @@
  *   key(c) = node_index(c) * members + member_rank(c)
  * is a bijection onto [0, nchunks): the prefix sum of the level-l item
  * counts in key order gives every segment's destination, and node i's
- * buffer starts at the prefix of its first key. One pass scatters counts
- * into key order, one CTA per level scans them, and a warp per segment
+ * buffer starts at the prefix of its first key. One pass writes the
+ * level-0 node table and scatters the counts of the levels above into key
+ * order, one CTA per level scans them, and a warp per segment
  * copies it with 8-byte vector moves (one splat per lane per step, eight
  * loads in flight per lane) into the group arena.
  *
@@ -62,25 +63,39 @@ __device__ __forceinline__ uint32_t group_key(const GroupGeom &g, uint32_t c, ui
 	return (*node_index << (g.eb[0] + g.eb[1] + g.eb[2])) | *rank;
 }
 
-/* counts[l][key(c)] = level-l splat items of chunk c (int16 units) */
-__global__ void k_group_scatter(const ChunkOut *__restrict__ outs, uint32_t nchunks, GroupArgs a)
+/* One thread per chunk c and level l (all kMaxLevels levels):
+ *   level 0: node c is chunk c, its list the chunk's level-0 segment in the
+ *   splat arena;
+ *   levels 1..lod_max: counts[l][key(c)] = the chunk's level-l splat items
+ *   (int16 units), and the node table entry cleared (k_group_copy records
+ *   the nodes that exist);
+ *   levels above lod_max: the node table entry cleared. */
+__global__ void k_group_tables(const ChunkOut *__restrict__ outs, uint32_t nchunks, int lod_max, GroupArgs a)
 {
 	const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
 	const int l = blockIdx.y;
 	if (c >= nchunks) return;
+	if (l == 0) {
+		a.node_off[c] = outs[c].svl_off;
+		a.node_items[c] = outs[c].svl_items[0];
+		return;
+	}
+	a.node_items[(size_t)l * nchunks + c] = 0;
+	if (l > lod_max) return;
 	const GroupGeom g = group_geom(a.max_bitw, l);
 	uint32_t node, rank;
 	const uint32_t key = group_key(g, c, &node, &rank);
 	a.counts[(size_t)l * nchunks + key] = outs[c].svl_items[l];
 }
 
-/* exclusive prefix sum of each level's counts, one CTA per level */
+/* exclusive prefix sum of each level's counts, one CTA per level >= 1 */
 __global__ void __launch_bounds__(1024) k_group_scan(uint32_t n, GroupArgs a)
 {
 	__shared__ uint64_t wsum[32];
 	__shared__ uint64_t wexcl[32];
 	__shared__ uint64_t s_tile, s_carry;
-	uint64_t *v = a.counts + (size_t)blockIdx.x * n;
+	const int l = 1 + (int)blockIdx.x;
+	uint64_t *v = a.counts + (size_t)l * n;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 	if (threadIdx.x == 0) s_carry = 0;
 	__syncthreads();
@@ -112,17 +127,7 @@ __global__ void __launch_bounds__(1024) k_group_scan(uint32_t n, GroupArgs a)
 		if (threadIdx.x == 0) s_carry += s_tile;
 		__syncthreads();
 	}
-	if (threadIdx.x == 0) a.level_total[blockIdx.x] = s_carry;
-}
-
-/* level 0: node c is chunk c, its list the chunk's level-0 segment in the
- * splat arena */
-__global__ void k_group_level0(const ChunkOut *__restrict__ outs, uint32_t nchunks, GroupArgs a)
-{
-	const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-	if (c >= nchunks) return;
-	a.node_off[c] = outs[c].svl_off;
-	a.node_items[c] = outs[c].svl_items[0];
+	if (threadIdx.x == 0) a.level_total[l] = s_carry;
 }
 
 /* levels >= 1: one warp per (chunk, level) segment, grid-stride: the warp
@@ -179,10 +184,9 @@ cudaError_t launch_group(const ChunkOut *outs, uint32_t nchunks, int lod_max, co
 {
 	if (!nchunks) return cudaSuccess;
 	const int L = lod_max + 1;
-	k_group_level0<<<(nchunks + 255) / 256, 256, 0, st>>>(outs, nchunks, a);
+	k_group_tables<<<dim3((nchunks + 255) / 256, kMaxLevels), 256, 0, st>>>(outs, nchunks, lod_max, a);
 	if (L > 1) {
-		k_group_scatter<<<dim3((nchunks + 255) / 256, L), 256, 0, st>>>(outs, nchunks, a);
-		k_group_scan<<<L, 1024, 0, st>>>(nchunks, a);
+		k_group_scan<<<L - 1, 1024, 0, st>>>(nchunks, a);
 		/* 8 warps per CTA, up to 8 CTAs per SM of a 152-SM GPU */
 		const uint64_t nseg = (uint64_t)nchunks * (uint64_t)(L - 1);
 		const uint32_t grid = (uint32_t)std::min<uint64_t>((nseg + 7) / 8, 152u * 8u);
