@@ -918,7 +918,7 @@ static int enqueue_rebuild(vp_world *w, int lod_max, unsigned flags)
 		Lg.n_items = w->n_geo;
 		e = launch_geometry(w->root_bitw, Lg, st);
 		if (e != cudaSuccess) return cuda_fail(e, "geometry launch");
-		w->launches += 2 + (L.n_uni ? 1 : 0); /* shell, single-run shells, geometry */
+		w->launches += 2; /* shell (single-run chunks in its last CTAs), geometry */
 	}
 	if (ctx->timing) cudaEventRecord(e2, st);
 	w->grouped_lod = -1;
@@ -1370,9 +1370,9 @@ static int stream_rebuild(vp_world *w, int lod_max, unsigned flags, int slabs, v
 		CK(cudaGetLastError());
 		CK(cudaEventRecord(w->slab_ev[k], st));
 	}
-	/* cursors, shell, single-run shells, and per slab geometry and the
-	 * cursor snapshot */
-	w->launches += 2 + (L.n_uni ? 1 : 0) + 2 * slabs;
+	/* cursors, shell (single-run chunks in its last CTAs), and per slab
+	 * geometry and the cursor snapshot */
+	w->launches += 2 + 2 * slabs;
 	w->grouped_lod = -1;
 	if ((flags & VP_REBUILD_GROUP) && (rc = enqueue_group(w, lod_max, limit[0]))) return rc;
 	w->last_lod = lod_max;

@@ -373,18 +373,55 @@ __device__ bool load_decoded(const uint8_t *src, const Smem &m, uint64_t *bar, u
 
 /* ------------------------------------------------------------------ */
 /* Shell pass                                                          */
+/* The shell of a single-run chunk (one run of R^3 voxels and the
+ * terminator), without decoding, by one warp: an all-air chunk has none
+ * (its neighbours see air); a solid one has every boundary bit set and its
+ * run's colour on the three low planes, as the decode path writes them. An
+ * item flagged kItemEmpty (all air, with all-air or no +x, +y and +z
+ * neighbours) gets no geometry pass: its result record is zeroed here, as
+ * the geometry pass would write it. */
+template <int RB>
+__device__ __forceinline__ void shell_uniform_item(const SetDesc *__restrict__ sets, const WorkItem &wi, ChunkOut *outs)
+{
+	using G = Geo<RB>;
+	constexpr uint32_t N = (uint32_t)G::R * G::R * G::R;
+	const int lane = threadIdx.x & 31;
+	if (wi.flags & kItemEmpty) {
+		static_assert(sizeof(ChunkOut) % 4 == 0, "result records are whole words");
+		uint32_t *o = (uint32_t *)(outs + wi.slot);
+		for (int i = lane; i < (int)(sizeof(ChunkOut) / 4); i += 32) o[i] = 0u;
+		return;
+	}
+	const SetDesc *S = sets + wi.set;
+	if (S->len[wi.chunk] != 2u) return;
+	const uint32_t w0 = S->pool[S->off[wi.chunk]];
+	if (w0 == N) return;
+	uint64_t *bits = S->shell_bits + (size_t)wi.chunk * G::shell_words;
+	for (int i = lane; i < (int)G::shell_words; i += 32) bits[i] = G::MASK;
+	uint32_t *cols = (uint32_t *)(S->shell_col + (size_t)wi.chunk * G::shell_cols);
+	const uint32_t c4 = (w0 >> 24) * 0x01010101u;
+	for (int i = lane; i < (int)(G::shell_cols / 4); i += 32) cols[i] = c4;
+}
+
 /* ------------------------------------------------------------------ */
 
 template <int RB>
 __global__ void __launch_bounds__(512, 2) k_shell(const SetDesc *__restrict__ sets, const WorkItem *__restrict__ items,
-					       uint32_t nitems, uint8_t *decoded, const uint32_t *__restrict__ dec_slot)
+					       uint32_t nitems, uint8_t *decoded, const uint32_t *__restrict__ dec_slot,
+					       const WorkItem *__restrict__ uni_items, uint32_t n_uni, ChunkOut *outs)
 {
 	using G = Geo<RB>;
 	constexpr int R = G::R, RR = G::RR;
 	extern __shared__ __align__(16) uint8_t smem[];
 	const Smem m = carve<RB>(smem);
 	const uint32_t it = blockIdx.x;
-	if (it >= nitems) return;
+	if (it >= nitems) {
+		/* the CTAs past the decoded chunks: a single-run chunk per warp
+		 * (they run in the launch's last wave) */
+		const uint32_t u = (it - nitems) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+		if (u < n_uni) shell_uniform_item<RB>(sets, uni_items[u], outs);
+		return;
+	}
 	const WorkItem wi = items[it];
 	const SetDesc S = sets[wi.set];
 	const uint32_t N = (uint32_t)R * R * R;
@@ -441,41 +478,6 @@ __global__ void __launch_bounds__(512, 2) k_shell(const SetDesc *__restrict__ se
 		cols[2 * RR + i] = s2 ? (uint8_t)(w2 >> 24) : (uint8_t)0;
 	}
 	if (ds != kNoSlot) store_decoded_wait();
-}
-
-/* Shells of single-run chunks (one run of R^3 voxels and the terminator),
- * without decoding: an all-air chunk has none (its neighbours see air); a
- * solid one has every boundary bit set and its run's colour on the three
- * low planes, as k_shell would write them. One warp per chunk; a chunk of
- * more than one run is left to k_shell. An item flagged kItemEmpty (all
- * air, with all-air or no +x, +y and +z neighbours) gets no geometry pass:
- * its result record is zeroed here, as the geometry pass would write it. */
-template <int RB>
-__global__ void __launch_bounds__(256) k_shell_uniform(const SetDesc *__restrict__ sets,
-						       const WorkItem *__restrict__ items, uint32_t nitems,
-						       ChunkOut *outs)
-{
-	using G = Geo<RB>;
-	constexpr uint32_t N = (uint32_t)G::R * G::R * G::R;
-	const uint32_t it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	const int lane = threadIdx.x & 31;
-	if (it >= nitems) return;
-	const WorkItem wi = items[it];
-	if (wi.flags & kItemEmpty) {
-		static_assert(sizeof(ChunkOut) % 4 == 0, "result records are whole words");
-		uint32_t *o = (uint32_t *)(outs + wi.slot);
-		for (int i = lane; i < (int)(sizeof(ChunkOut) / 4); i += 32) o[i] = 0u;
-		return;
-	}
-	const SetDesc *S = sets + wi.set;
-	if (S->len[wi.chunk] != 2u) return;
-	const uint32_t w0 = S->pool[S->off[wi.chunk]];
-	if (w0 == N) return;
-	uint64_t *bits = S->shell_bits + (size_t)wi.chunk * G::shell_words;
-	for (int i = lane; i < (int)G::shell_words; i += 32) bits[i] = G::MASK;
-	uint32_t *cols = (uint32_t *)(S->shell_col + (size_t)wi.chunk * G::shell_cols);
-	const uint32_t c4 = (w0 >> 24) * 0x01010101u;
-	for (int i = lane; i < (int)(G::shell_cols / 4); i += 32) cols[i] = c4;
 }
 
 /* ------------------------------------------------------------------ */
@@ -1643,14 +1645,12 @@ static cudaError_t launch_rb(const GeoLaunch &L, cudaStream_t st)
 	if (e != cudaSuccess) return e;
 	e = cudaFuncSetAttribute(k_geometry<RB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::bytes);
 	if (e != cudaSuccess) return e;
-	if (L.run_shell && L.n_shell) {
-		k_shell<RB><<<L.n_shell, L.threads, G::bytes, st>>>(L.sets, L.shell_items, L.n_shell, L.decoded,
-								     L.dec_slot);
-		e = cudaGetLastError();
-		if (e != cudaSuccess) return e;
-	}
-	if (L.run_shell && L.n_uni) {
-		k_shell_uniform<RB><<<(L.n_uni + 7) / 8, 256, 0, st>>>(L.sets, L.uni_items, L.n_uni, L.outs);
+	if (L.run_shell && (L.n_shell || L.n_uni)) {
+		/* the decoded chunks, then the single-run ones a warp each */
+		const uint32_t warps = (uint32_t)L.threads / 32u;
+		const uint32_t grid = L.n_shell + (L.n_uni + warps - 1u) / warps;
+		k_shell<RB><<<grid, L.threads, G::bytes, st>>>(L.sets, L.shell_items, L.n_shell, L.decoded, L.dec_slot,
+							       L.uni_items, L.n_uni, L.outs);
 		e = cudaGetLastError();
 		if (e != cudaSuccess) return e;
 	}

@@ -138,7 +138,7 @@ struct vp_world {
 	std::vector<uint8_t> hnull;              /* host copy; empty = to be fetched */
 	/* shell pass order: the chunks of more than one run (or with a handoff
 	 * slot), longest first, then the single-run chunks, whose shells (if
-	 * not all air) k_shell_uniform writes */
+	 * not all air) the shell launch's last CTAs write a warp each */
 	WorkItem *d_shell_items = nullptr;
 	uint32_t n_shell_multi = 0;
 	std::vector<uint8_t> modes;
