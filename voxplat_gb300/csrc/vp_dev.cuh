@@ -23,6 +23,31 @@ namespace vp {
 constexpr int kMaxLevels = 8;   /* LOD levels 0..7 */
 constexpr unsigned kFull = 0xFFFFFFFFu;
 
+/* Programmatic dependent launch (sm_90 and later): a kernel launched with
+ * launch_dependent() may start while the kernel before it on the stream is
+ * finishing; it calls grid_wait() before touching anything that kernel
+ * writes (the wait returns at once for an ordinary launch). A kernel calls
+ * grid_release() to let the next one start launching early. */
+__device__ __forceinline__ void grid_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void grid_release() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
+template <typename... P, typename... A>
+static inline cudaError_t launch_dependent(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+					   A &&...args)
+{
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = grid;
+	cfg.blockDim = block;
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = st;
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	at[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = at;
+	cfg.numAttrs = 1;
+	return cudaLaunchKernelEx(&cfg, k, static_cast<P>(args)...);
+}
+
 struct SetDesc {
 	const uint32_t *pool;
 	const uint64_t *off;

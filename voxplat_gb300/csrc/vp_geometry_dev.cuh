@@ -414,6 +414,8 @@ __global__ void __launch_bounds__(512, 2) k_shell(const SetDesc *__restrict__ se
 	constexpr int R = G::R, RR = G::RR;
 	extern __shared__ __align__(16) uint8_t smem[];
 	const Smem m = carve<RB>(smem);
+	/* the geometry pass may start launching once the last wave is on */
+	grid_release();
 	const uint32_t it = blockIdx.x;
 	if (it >= nitems) {
 		/* the CTAs past the decoded chunks: a single-run chunk per warp
@@ -1559,6 +1561,8 @@ __global__ void __launch_bounds__(512, 2) k_geometry(const SetDesc *__restrict__
 	extern __shared__ __align__(16) uint8_t smem[];
 	const Smem m = carve<RB>(smem);
 	__shared__ uint32_t s_item;
+	grid_wait(); /* the shell pass's shells and handed-over chunks */
+	grid_release();
 	__shared__ __align__(8) uint64_t s_bar; /* completion of the decoded-chunk bulk copies */
 	__shared__ uint32_t s_flag;             /* a bounded wait ran out */
 	uint32_t phase = 0;
@@ -1656,8 +1660,9 @@ static cudaError_t launch_rb(const GeoLaunch &L, cudaStream_t st)
 	}
 	if (L.n_items) {
 		const uint32_t grid = L.queue ? L.ctas : L.n_items;
-		k_geometry<RB><<<grid, L.threads, G::bytes, st>>>(L.sets, L.items, L.n_items, L.queue, L.outs, L.svl, L.vbo,
-								 L.ibo, L.lod_max, L.decoded, L.dec_slot);
+		e = launch_dependent(k_geometry<RB>, dim3(grid), dim3(L.threads), G::bytes, st, L.sets, L.items,
+				     L.n_items, L.queue, L.outs, L.svl, L.vbo, L.ibo, L.lod_max, L.decoded, L.dec_slot);
+		if (e != cudaSuccess) return e;
 		e = cudaGetLastError();
 	}
 	return e;

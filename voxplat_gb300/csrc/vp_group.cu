@@ -72,6 +72,8 @@ __device__ __forceinline__ uint32_t group_key(const GroupGeom &g, uint32_t c, ui
  *   levels above lod_max: the node table entry cleared. */
 __global__ void k_group_tables(const ChunkOut *__restrict__ outs, uint32_t nchunks, int lod_max, GroupArgs a)
 {
+	grid_wait(); /* the geometry pass's result records */
+	grid_release();
 	const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
 	const int l = blockIdx.y;
 	if (c >= nchunks) return;
@@ -94,6 +96,8 @@ __global__ void __launch_bounds__(1024) k_group_scan(uint32_t n, GroupArgs a)
 	__shared__ uint64_t wsum[32];
 	__shared__ uint64_t wexcl[32];
 	__shared__ uint64_t s_tile, s_carry;
+	grid_wait(); /* the scattered counts */
+	grid_release();
 	const int l = 1 + (int)blockIdx.x;
 	uint64_t *v = a.counts + (size_t)l * n;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -138,6 +142,7 @@ __global__ void __launch_bounds__(1024) k_group_scan(uint32_t n, GroupArgs a)
 __global__ void __launch_bounds__(256) k_group_copy(const ChunkOut *__restrict__ outs, uint32_t nchunks, int levels,
 						    GroupArgs a)
 {
+	grid_wait(); /* the scanned counts */
 	const int lane = threadIdx.x & 31;
 	const uint64_t nseg = (uint64_t)nchunks * (uint64_t)levels;
 	const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
@@ -184,13 +189,17 @@ cudaError_t launch_group(const ChunkOut *outs, uint32_t nchunks, int lod_max, co
 {
 	if (!nchunks) return cudaSuccess;
 	const int L = lod_max + 1;
-	k_group_tables<<<dim3((nchunks + 255) / 256, kMaxLevels), 256, 0, st>>>(outs, nchunks, lod_max, a);
+	cudaError_t e = launch_dependent(k_group_tables, dim3((nchunks + 255) / 256, kMaxLevels), dim3(256), 0, st,
+					 outs, nchunks, lod_max, a);
+	if (e != cudaSuccess) return e;
 	if (L > 1) {
-		k_group_scan<<<L - 1, 1024, 0, st>>>(nchunks, a);
+		e = launch_dependent(k_group_scan, dim3(L - 1), dim3(1024), 0, st, nchunks, a);
+		if (e != cudaSuccess) return e;
 		/* 8 warps per CTA, up to 8 CTAs per SM of a 152-SM GPU */
 		const uint64_t nseg = (uint64_t)nchunks * (uint64_t)(L - 1);
 		const uint32_t grid = (uint32_t)std::min<uint64_t>((nseg + 7) / 8, 152u * 8u);
-		k_group_copy<<<grid, 256, 0, st>>>(outs, nchunks, L - 1, a);
+		e = launch_dependent(k_group_copy, dim3(grid), dim3(256), 0, st, outs, nchunks, L - 1, a);
+		if (e != cudaSuccess) return e;
 	}
 	return cudaGetLastError();
 }
