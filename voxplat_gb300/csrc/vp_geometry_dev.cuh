@@ -1023,18 +1023,21 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
 			   ChunkOut *out, const Arena &avbo, const Arena &aibo)
 {
 	using G = Geo<RB>;
-	constexpr int R = G::R, RR = G::RR, NG = (RR + 31) / 32;
+	constexpr int R = G::R, RR = G::RR, NG = (RR + 63) / 64; /* 64-row groups, two rows a lane */
 	__shared__ unsigned long long s_base[2];
 	__shared__ uint32_t s_ok, s_next;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-	/* pass 1: faces per 32-row group */
+	/* pass 1: faces per 64-row group */
 	for (int g = warp; g < NG; g += nw) {
-		const int r = g * 32 + lane;
 		uint32_t c = 0;
-		if (r < RR) {
-			uint64_t fx, fy, fz;
-			face_bits<RB>(m, r & (R - 1), r >> RB, fx, fy, fz);
-			c = __popcll(fx) + __popcll(fy) + __popcll(fz);
+#pragma unroll
+		for (int h = 0; h < 2; h++) {
+			const int r = g * 64 + 2 * lane + h;
+			if (r < RR) {
+				uint64_t fx, fy, fz;
+				face_bits<RB>(m, r & (R - 1), r >> RB, fx, fy, fz);
+				c += __popcll(fx) + __popcll(fy) + __popcll(fz);
+			}
 		}
 		c = __reduce_add_sync(kFull, c);
 		if (lane == 0) m.grp[g] = c;
@@ -1066,19 +1069,30 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
 	int16_t *vbo = (int16_t *)avbo.base + s_base[0] * 8u;
 	uint32_t *ibo = (uint32_t *)aibo.base + s_base[1] * 4u;
 	const SmallAcc<RB> acc{S, stream, m};
-	/* pass 2: warps take the non-empty 32-row groups from a shared counter;
-	 * one face per lane per step (a second face per step, with both
-	 * searches first, measured slower) */
+	/* pass 2: warps take the non-empty groups from a shared counter; lane s
+	 * holds the face counts of rows 2s and 2s + 1, and the lane that emits
+	 * a face recomputes its row's three face words (cheaper than shuffling
+	 * six words a step); one face per lane per step (a second face per
+	 * step, with both searches first, measured slower) */
 	for (;;) {
 		uint32_t t = 0;
 		if (lane == 0) t = atomicAdd(&s_next, 1u);
 		t = __shfl_sync(kFull, t, 0);
 		if (t >= listed) break;
 		const uint32_t g = m.glist[t];
-		const int r = (int)g * 32 + lane;
-		uint64_t fx = 0, fy = 0, fz = 0;
-		if (r < RR) face_bits<RB>(m, r & (R - 1), r >> RB, fx, fy, fz);
-		const uint32_t c = __popcll(fx) + __popcll(fy) + __popcll(fz);
+		const int r0 = (int)g * 64 + 2 * lane;
+		uint32_t ca = 0, cb = 0;
+		if (r0 < RR) {
+			uint64_t fx, fy, fz;
+			face_bits<RB>(m, r0 & (R - 1), r0 >> RB, fx, fy, fz);
+			ca = __popcll(fx) + __popcll(fy) + __popcll(fz);
+		}
+		if (r0 + 1 < RR) {
+			uint64_t fx, fy, fz;
+			face_bits<RB>(m, (r0 + 1) & (R - 1), (r0 + 1) >> RB, fx, fy, fz);
+			cb = __popcll(fx) + __popcll(fy) + __popcll(fz);
+		}
+		const uint32_t c = ca + cb;
 		const uint32_t inc = warp_incl_add(c);
 		const uint32_t excl = inc - c;
 		const uint32_t T = __shfl_sync(kFull, inc, 31);
@@ -1086,12 +1100,16 @@ __device__ void mesh_chunk(const SetDesc &S, const uint32_t *__restrict__ stream
 		for (uint32_t k = 0; k < T; k += 32) {
 			const uint32_t j0 = k + lane;
 			const int s0 = search_lane(excl, j0);
-			const uint32_t e0 = __shfl_sync(kFull, excl, s0);
-			const uint64_t ax = shfl64(fx, s0), ay = shfl64(fy, s0), az = shfl64(fz, s0);
+			const uint32_t e0 = __shfl_sync(kFull, excl, s0), a0 = __shfl_sync(kFull, ca, s0);
 			if (j0 < T) {
+				uint32_t kk = j0 - e0;
+				const bool second = kk >= a0;
+				kk -= second ? a0 : 0u;
+				const int rr = (int)g * 64 + 2 * s0 + (second ? 1 : 0);
+				uint64_t ax, ay, az;
+				face_bits<RB>(m, rr & (R - 1), rr >> RB, ax, ay, az);
 				int x, i;
-				select_face<RB>(ax, ay, az, j0 - e0, x, i);
-				const int rr = (int)g * 32 + s0;
+				select_face<RB>(ax, ay, az, kk, x, i);
 				emit_face<RB>(acc, S, cv, x, rr & (R - 1), rr >> RB, i, base + j0, vbo, ibo);
 			}
 		}
