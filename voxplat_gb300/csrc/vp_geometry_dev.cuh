@@ -667,9 +667,9 @@ struct LevelTab {
 };
 
 /* Rows per emission group of level l: 32, one per lane, except level 0 of
- * chunks up to 64^3, whose groups are 64 rows, two consecutive rows per
- * lane (half the groups to set up, and fewer partly filled steps). */
-constexpr int group_rows(int rb, int l) { return (l == 0 && rb <= 6) ? 64 : 32; }
+ * chunks up to 64^3, whose groups are 96 rows, three consecutive rows per
+ * lane (a third of the groups to set up, and fewer partly filled steps). */
+constexpr int group_rows(int rb, int l) { return (l == 0 && rb <= 6) ? 96 : 32; }
 
 constexpr LevelTab make_level_tab()
 {
@@ -1350,24 +1350,24 @@ __device__ __forceinline__ void splat_group(const SetDesc &S, const uint32_t *__
 	}
 }
 
-/* Pass 2 of one non-empty 64-row level-0 group (three quarters of the
- * splats): lane s holds rows 2s and 2s + 1, consecutive in the item order,
- * and the pair's exclusive item offset. An item's row follows from the
- * pair's first count, its (y, z) from the row index. The loop is
+/* Pass 2 of one non-empty 96-row level-0 group (three quarters of the
+ * splats): lane s holds rows 3s .. 3s + 2, consecutive in the item order,
+ * and their exclusive item offset. An item's row follows from the first two
+ * rows' counts, its (y, z) from the row index. The loop is
  * software-pipelined: a step's colour and shadow loads are issued, and
  * consumed one step later, after the next step's search and select. */
 template <int RB>
 __device__ __forceinline__ void splat_group_l0(const SetDesc &S, const uint32_t *__restrict__ stream, const Smem &m,
 					       const uint32_t cv[3], int g, int16_t *dst, bool sh_in)
 {
-	static_assert(group_rows(RB, 0) == 64, "level-0 groups of two rows a lane");
 	constexpr int R = Geo<RB>::R;
 	constexpr uint32_t n = (uint32_t)R + 1u;
 	const int lane = threadIdx.x & 31;
-	const uint32_t rbase = (uint32_t)(g - c_lv.gstart[RB][0]) * 64u;
-	const uint32_t r0 = rbase + 2u * (uint32_t)lane;
-	uint64_t ra = 0, rb = 0;
-	uint32_t ca = 0, cb = 0;
+	static_assert(group_rows(RB, 0) == 96, "level-0 groups of three rows a lane");
+	const uint32_t rbase = (uint32_t)(g - c_lv.gstart[RB][0]) * 96u;
+	const uint32_t r0 = rbase + 3u * (uint32_t)lane;
+	uint64_t ra = 0, rb = 0, rc = 0;
+	uint32_t ca = 0, cb = 0, cc = 0;
 	if (r0 < n * n) {
 		const uint32_t z = r0 / n, y = r0 - z * n;
 		uint32_t xr;
@@ -1380,29 +1380,46 @@ __device__ __forceinline__ void splat_group_l0(const SetDesc &S, const uint32_t 
 		rb = e0_row<RB>(m, (int)y, (int)z, xr);
 		cb = __popcll(rb) + xr;
 	}
-	const uint32_t c = ca + cb;
+	if (r0 + 2u < n * n) {
+		const uint32_t z = (r0 + 2u) / n, y = (r0 + 2u) - z * n;
+		uint32_t xr;
+		rc = e0_row<RB>(m, (int)y, (int)z, xr);
+		cc = __popcll(rc) + xr;
+	}
+	const uint32_t c = ca + cb + cc;
 	const uint32_t inc = warp_incl_add(c);
 	const uint32_t excl = inc - c;
 	const uint32_t T = __shfl_sync(kFull, inc, 31);
 	const uint32_t base = m.grp[g];
+	const uint32_t cab = ca | (cb << 8); /* row counts are at most R + 1 */
 	SplatPend pend;
 	bool pv = false;
 	uint32_t pj = 0;
 	for (uint32_t k = 0; k < T; k += 32) {
 		const uint32_t j0 = k + lane;
 		const int s0 = search_lane(excl, j0);
-		const uint32_t e0 = __shfl_sync(kFull, excl, s0), a0 = __shfl_sync(kFull, ca, s0);
-		const uint64_t wa = shfl64(ra, s0), wb = shfl64(rb, s0);
+		const uint32_t e0 = __shfl_sync(kFull, excl, s0), p0 = __shfl_sync(kFull, cab, s0);
+		const uint64_t wa = shfl64(ra, s0), wb = shfl64(rb, s0), wc = shfl64(rc, s0);
 		const bool v = j0 < T;
 		int x = 0, y = 0, z = 0;
 		if (v) {
 			int kk = (int)(j0 - e0);
-			const bool second = kk >= (int)a0;
-			const uint64_t w = second ? wb : wa;
-			kk = second ? kk - (int)a0 : kk;
+			const int a0 = (int)(p0 & 0xFFu), b0 = (int)(p0 >> 8);
+			uint32_t i = 0;
+			uint64_t w = wa;
+			if (kk >= a0) {
+				kk -= a0;
+				i = 1;
+				w = wb;
+				if (kk >= b0) {
+					kk -= b0;
+					i = 2;
+					w = wc;
+				}
+			}
 			/* the x = R cell is its row's last item */
 			x = kk < __popcll(w) ? select_bit(w, kk) : R;
-			const uint32_t r = rbase + 2u * (uint32_t)s0 + (second ? 1u : 0u);
+			const uint32_t r = rbase + 3u * (uint32_t)s0 + i;
 			z = (int)(r / n);
 			y = (int)(r - (uint32_t)z * n);
 		}
