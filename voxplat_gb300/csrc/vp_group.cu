@@ -18,9 +18,10 @@
  * counts in key order gives every segment's destination, and node i's
  * buffer starts at the prefix of its first key. One pass writes the
  * level-0 node table and scatters the counts of the levels above into key
- * order, one CTA per level scans them, and a warp per segment
- * copies it with 8-byte vector moves (one splat per lane per step, eight
- * loads in flight per lane) into the group arena.
+ * order, one CTA per level scans them, and a warp per segment (in a
+ * small world, per eighth of a large level-1 segment) copies it with
+ * 8-byte vector moves (one splat per lane per step, eight loads in flight
+ * per lane) into the group arena.
  *
  * A rebuild whose splat arena overflowed left some chunks without lists
  * (their records carry the overflow status); the copy is then skipped as a
@@ -134,22 +135,36 @@ __global__ void __launch_bounds__(1024) k_group_scan(uint32_t n, GroupArgs a)
 	if (threadIdx.x == 0) a.level_total[l] = s_carry;
 }
 
-/* levels >= 1: one warp per (chunk, level) segment, grid-stride: the warp
- * copies the chunk's level-l segment to its node's place, one splat (8
- * bytes) per lane per step; the first member of each node also records the
- * node's offset and length. (A CTA per segment spent most of its time on
- * launching CTAs for the many empty segments of worlds with air layers.) */
+/* A level-1 segment (the largest) of at least kSliceMin splats is copied in
+ * up to kL1Slices slices, one warp each, when the world has few segments for
+ * the GPU's warps (the largest segments then set the copy's time); other
+ * segments, and every segment of a large world, by one warp each. */
+constexpr uint32_t kL1Slices = 8, kSliceMin = 1024;
+
+/* levels >= 1: one warp per work unit, grid-stride: a slice of a chunk's
+ * level-1 segment (l1_slices per chunk), or a chunk's whole segment of a
+ * level >= 2. The warp copies it to its node's place, one splat (8 bytes)
+ * per lane per step; the first unit of each node's first member also
+ * records the node's offset and length. (A CTA per segment spent most of
+ * its time on launching CTAs for the many empty segments of worlds with air
+ * layers.) */
 __global__ void __launch_bounds__(256) k_group_copy(const ChunkOut *__restrict__ outs, uint32_t nchunks, int levels,
-						    GroupArgs a)
+						    uint32_t l1_slices, GroupArgs a)
 {
 	grid_wait(); /* the scanned counts */
 	const int lane = threadIdx.x & 31;
-	const uint64_t nseg = (uint64_t)nchunks * (uint64_t)levels;
+	const uint32_t per_chunk = l1_slices + (uint32_t)(levels - 1);
+	const uint64_t nwork = (uint64_t)nchunks * per_chunk;
 	const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
 	if (*a.svl_cursor > a.svl_cap_units) return; /* overflowed rebuild: rerun follows */
-	for (uint64_t seg = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); seg < nseg; seg += nwarps) {
-		const int l = 1 + (int)(seg % (uint64_t)levels);
-		const uint32_t c = (uint32_t)(seg / (uint64_t)levels);
+	for (uint64_t wu = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); wu < nwork; wu += nwarps) {
+		const uint32_t c = (uint32_t)(wu / per_chunk), j = (uint32_t)(wu % per_chunk);
+		const int l = j < l1_slices ? 1 : 1 + (int)(j - l1_slices + 1u);
+		const uint32_t slice = j < l1_slices ? j : 0u;
+		const uint32_t items = outs[c].svl_items[l];
+		const uint32_t n = items / 4u; /* splats */
+		const uint32_t nslices = (l == 1 && n >= kSliceMin) ? l1_slices : 1u;
+		if (slice >= nslices) continue; /* a small segment: its first slice copies it */
 		const GroupGeom g = group_geom(a.max_bitw, l);
 		uint32_t node, rank;
 		const uint32_t key = group_key(g, c, &node, &rank);
@@ -157,31 +172,31 @@ __global__ void __launch_bounds__(256) k_group_copy(const ChunkOut *__restrict__
 		for (int k = 1; k < l; k++) lbase += a.level_total[k];
 		const uint64_t *cnt = a.counts + (size_t)l * nchunks;
 		const uint64_t dst_off = lbase + cnt[key];
-		if (rank == 0 && lane == 0) {
+		if (slice == 0 && rank == 0 && lane == 0) {
 			const uint32_t mbits = g.eb[0] + g.eb[1] + g.eb[2];
 			const uint32_t next_key = (node + 1u) << mbits;
 			const uint64_t end = next_key < nchunks ? cnt[next_key] : a.level_total[l];
 			a.node_off[(size_t)l * nchunks + node] = dst_off;
 			a.node_items[(size_t)l * nchunks + node] = (uint32_t)(end - cnt[key]);
 		}
-		const uint32_t items = outs[c].svl_items[l];
 		if (!items) continue;
 		uint64_t src_off = outs[c].svl_off;
 		for (int k = 0; k < l; k++) src_off += outs[c].svl_items[k];
 		if (src_off + items > a.svl_cap_units * 8u || dst_off + items > a.out_cap) continue;
 		const uint2 *src = (const uint2 *)(a.svl + src_off);
 		uint2 *dst = (uint2 *)(a.out + dst_off);
-		const uint32_t n = items / 4u;
+		const uint32_t lo = (uint32_t)((uint64_t)n * slice / nslices);
+		const uint32_t hi = (uint32_t)((uint64_t)n * (slice + 1u) / nslices);
 		/* eight loads in flight per lane before their stores */
-		uint32_t s = lane;
-		for (; s + 224u < n; s += 256u) {
+		uint32_t s = lo + (uint32_t)lane;
+		for (; s + 224u < hi; s += 256u) {
 			uint2 v[8];
 #pragma unroll
 			for (int u = 0; u < 8; u++) v[u] = __ldg(src + s + 32u * u);
 #pragma unroll
 			for (int u = 0; u < 8; u++) dst[s + 32u * u] = v[u];
 		}
-		for (; s < n; s += 32u) dst[s] = __ldg(src + s);
+		for (; s < hi; s += 32u) dst[s] = __ldg(src + s);
 	}
 }
 
@@ -195,10 +210,14 @@ cudaError_t launch_group(const ChunkOut *outs, uint32_t nchunks, int lod_max, co
 	if (L > 1) {
 		e = launch_dependent(k_group_scan, dim3(L - 1), dim3(1024), 0, st, nchunks, a);
 		if (e != cudaSuccess) return e;
-		/* 8 warps per CTA, up to 8 CTAs per SM of a 152-SM GPU */
+		/* 8 warps per CTA, up to 8 CTAs per SM of a 152-SM GPU; level-1
+		 * slices while the segments are fewer than eight per warp */
 		const uint64_t nseg = (uint64_t)nchunks * (uint64_t)(L - 1);
-		const uint32_t grid = (uint32_t)std::min<uint64_t>((nseg + 7) / 8, 152u * 8u);
-		e = launch_dependent(k_group_copy, dim3(grid), dim3(256), 0, st, outs, nchunks, L - 1, a);
+		const uint32_t max_grid = 152u * 8u;
+		const uint32_t l1_slices = nseg <= (uint64_t)max_grid * 8u * 8u ? kL1Slices : 1u;
+		const uint64_t nwork = (uint64_t)nchunks * (l1_slices + (uint64_t)(L - 2));
+		const uint32_t grid = (uint32_t)std::min<uint64_t>((nwork + 7) / 8, max_grid);
+		e = launch_dependent(k_group_copy, dim3(grid), dim3(256), 0, st, outs, nchunks, L - 1, l1_slices, a);
 		if (e != cudaSuccess) return e;
 	}
 	return cudaGetLastError();
