@@ -104,9 +104,17 @@ __global__ void __launch_bounds__(1024) k_group_scan(uint32_t n, GroupArgs a)
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 	if (threadIdx.x == 0) s_carry = 0;
 	__syncthreads();
-	for (uint32_t base = 0; base < n; base += blockDim.x) {
-		const uint32_t i = base + threadIdx.x;
-		const uint64_t x = i < n ? v[i] : 0ull;
+	/* four consecutive counts a thread per tile */
+	constexpr uint32_t K = 4;
+	for (uint32_t base = 0; base < n; base += K * blockDim.x) {
+		const uint32_t i0 = base + K * threadIdx.x;
+		uint64_t xs[K];
+		uint64_t x = 0;
+#pragma unroll
+		for (uint32_t k = 0; k < K; k++) {
+			xs[k] = i0 + k < n ? v[i0 + k] : 0ull;
+			x += xs[k];
+		}
 		uint64_t inc = x;
 #pragma unroll
 		for (int d = 1; d < 32; d <<= 1) {
@@ -127,7 +135,12 @@ __global__ void __launch_bounds__(1024) k_group_scan(uint32_t n, GroupArgs a)
 			if (lane == 31) s_tile = wi;
 		}
 		__syncthreads();
-		if (i < n) v[i] = s_carry + wexcl[warp] + inc - x;
+		uint64_t run = s_carry + wexcl[warp] + inc - x;
+#pragma unroll
+		for (uint32_t k = 0; k < K; k++) {
+			if (i0 + k < n) v[i0 + k] = run;
+			run += xs[k];
+		}
 		__syncthreads();
 		if (threadIdx.x == 0) s_carry += s_tile;
 		__syncthreads();
